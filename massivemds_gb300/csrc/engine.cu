@@ -1,0 +1,624 @@
+// The CUDA engine behind the C ABI in include/mdsx.h.
+//
+// State machine of the MassiveMDS CPU engine (src/NewMultiDimensionalScaling.hpp),
+// restated for device-resident data:
+//   updateLocations  -> locations dirty (sum and gradient unknown)       (:134-166)
+//   setParameters    -> tau; with truncation both results dirty         (:262-274)
+//   getSumOfIncrements / getLogLikelihoodGradient -> one fused sweep if the
+//                       result is unknown; the sweep yields both results (:193-203, :281-302)
+//   storeState       -> copy locations, keep sums, tau (and the gradient) (:205-217)
+//   restoreState     -> swap locations back, restore sums as known, tau   (:234-255)
+//   acceptState      -> nothing to do for whole-matrix updates            (:226-232)
+//   makeDirty        -> both results unknown                             (:276-279)
+// Device layout: delta row-major [N][ld] (ld = N rounded up to 16 bytes),
+// locations SoA [P][x_ld] in the compute precision (two buffers: current and
+// stored), gradient [N][P] double (two buffers), scratch sized by the tile plan.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mdsx.h"
+#include "normal_rational.h"
+#include "sweep.h"
+
+using mdsx::KernelShape;
+using mdsx::Mode;
+using mdsx::SweepArgs;
+
+struct mdsx_engine {
+    int p = 0, n = 0;
+    long flags = 0;
+    int device = 0;
+    bool trunc = false;
+    Mode mode = Mode::kF64;
+    bool delta_f32 = false, x_f32 = false;
+
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+
+    KernelShape shape{};
+    int n_row_blocks = 0, rows_padded = 0, chunk_steps = 0, n_chunks = 0, n_tiles = 0, grid = 0;
+
+    void* d_delta = nullptr;
+    long long ld = 0;
+    void* d_x[2] = {nullptr, nullptr};
+    int x_ld = 0;
+    int xcur = 0;
+    double* d_xin = nullptr;
+    double* d_grad[2] = {nullptr, nullptr};
+    int gcur = 0;
+    double* d_out = nullptr;  // [0] r2, [1] logPhi, [2] sumOfIncrements, [3] error word (int)
+    void* d_gpart = nullptr;
+    double* d_lpart = nullptr;
+    double* d_lrow = nullptr;
+    unsigned* d_counts = nullptr;  // [n_row_blocks] + [1]
+    int* d_row_nan = nullptr;
+    double* h_out = nullptr;  // pinned mirror of d_out
+
+    CUtensorMap tmap_delta{};
+    CUtensorMap tmap_x[2]{};
+
+    bool data_set = false;
+    double tau = 0.0, stored_tau = 0.0;
+    bool sum_known = false;
+    double sum_r2 = 0.0, sum_log = 0.0;  // last computed (ordered-pair, unscaled) sums
+    double stored_sum_r2 = 0.0, stored_sum_log = 0.0;
+    bool grad_known = false, stored_grad_known = false;
+    int last_launches = 0;
+    std::string last_error;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(mdsx_engine* e, int code, const std::string& msg) {
+    if (e)
+        e->last_error = msg;
+    else
+        g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(mdsx_engine* e, cudaError_t err, const char* what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(err);
+    return fail(e, err == cudaErrorMemoryAllocation ? MDSX_ENOMEM : MDSX_ECUDA, msg);
+}
+
+#define MDSX_CUDA(e, call)                                \
+    do {                                                  \
+        cudaError_t _err = (call);                        \
+        if (_err != cudaSuccess) return cuda_fail(e, _err, #call); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            changed = cudaSetDevice(dev) == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+int make_tmap_2d(mdsx_engine* e, CUtensorMap* map, void* base, bool f32, long long cols, long long rows,
+                 long long ld_elems, unsigned box_cols, unsigned box_rows) {
+    auto fn = encode_tiled();
+    if (!fn) return fail(e, MDSX_ECUDA, "cuTensorMapEncodeTiled unavailable from the driver");
+    const int elem = f32 ? 4 : 8;
+    cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)(ld_elems * elem)};
+    cuuint32_t box[2] = {box_cols, box_rows};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, base, gdim,
+                    gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+        return fail(e, MDSX_ECUDA, buf);
+    }
+    return MDSX_OK;
+}
+
+void free_all(mdsx_engine* e) {
+    cudaFree(e->d_delta);
+    cudaFree(e->d_x[0]);
+    cudaFree(e->d_x[1]);
+    cudaFree(e->d_xin);
+    cudaFree(e->d_grad[0]);
+    cudaFree(e->d_grad[1]);
+    cudaFree(e->d_out);
+    cudaFree(e->d_gpart);
+    cudaFree(e->d_lpart);
+    cudaFree(e->d_lrow);
+    cudaFree(e->d_counts);
+    cudaFree(e->d_row_nan);
+    if (e->h_out) cudaFreeHost(e->h_out);
+    if (e->own_stream) cudaStreamDestroy(e->own_stream);
+}
+
+int plan_and_allocate(mdsx_engine* e) {
+    if (!mdsx::sweep_shape(e->mode, e->p, &e->shape))
+        return fail(e, MDSX_EUNSUPPORTED, "embedding dimension not built (1..MDSX_MAX_DIMENSION)");
+    int ctas = 0;
+    MDSX_CUDA(e, mdsx::sweep_occupancy(e->mode, e->p, e->trunc, &ctas));
+    if (ctas < 1) return fail(e, MDSX_ECUDA, "sweep kernel cannot be resident on this device");
+    const int rb = e->shape.rb;
+    e->n_row_blocks = (e->n + rb - 1) / rb;
+    e->rows_padded = e->n_row_blocks * rb;
+    const int steps_total = (e->n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+    const long long grid_max = (long long)e->sm_count * ctas;
+    // About 16 tiles per resident CTA, so the static round-robin tile order
+    // balances to within a few percent.
+    const long long target_tiles = 16 * grid_max;
+    long long chunks = (target_tiles + e->n_row_blocks - 1) / e->n_row_blocks;
+    chunks = std::max(1LL, std::min<long long>(chunks, steps_total));
+    e->chunk_steps = (int)((steps_total + chunks - 1) / chunks);
+    e->n_chunks = (steps_total + e->chunk_steps - 1) / e->chunk_steps;
+    e->n_tiles = e->n_row_blocks * e->n_chunks;
+    e->grid = (int)std::min<long long>(e->n_tiles, grid_max);
+
+    const int delta_elem = e->shape.delta_elem_bytes;
+    e->ld = round_up(e->n, 16 / delta_elem);
+    e->x_ld = (int)std::max<long long>(round_up(e->n, mdsx::kStepCols), e->rows_padded);
+    const size_t x_bytes = (size_t)e->p * e->x_ld * e->shape.x_elem_bytes;
+    const size_t acc_bytes = e->x_f32 ? 4 : 8;
+
+    MDSX_CUDA(e, cudaMalloc(&e->d_delta, (size_t)e->n * e->ld * delta_elem));
+    MDSX_CUDA(e, cudaMalloc(&e->d_x[0], x_bytes));
+    MDSX_CUDA(e, cudaMalloc(&e->d_x[1], x_bytes));
+    MDSX_CUDA(e, cudaMemsetAsync(e->d_x[0], 0, x_bytes, e->stream));
+    MDSX_CUDA(e, cudaMemsetAsync(e->d_x[1], 0, x_bytes, e->stream));
+    MDSX_CUDA(e, cudaMalloc(&e->d_xin, (size_t)e->n * e->p * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_grad[0], (size_t)e->n * e->p * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_grad[1], (size_t)e->n * e->p * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_out, 4 * sizeof(double)));
+    MDSX_CUDA(e, cudaMemsetAsync(e->d_out, 0, 4 * sizeof(double), e->stream));
+    MDSX_CUDA(e, cudaMalloc(&e->d_gpart, (size_t)e->n_chunks * e->rows_padded * e->p * acc_bytes));
+    MDSX_CUDA(e, cudaMalloc(&e->d_lpart, (size_t)e->n_tiles * mdsx::kConsumerWarps * 2 * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_lrow, (size_t)e->n_row_blocks * 2 * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_counts, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned)));
+    MDSX_CUDA(e, cudaMemsetAsync(e->d_counts, 0, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned), e->stream));
+    MDSX_CUDA(e, cudaMalloc(&e->d_row_nan, (size_t)e->rows_padded * sizeof(int)));
+    MDSX_CUDA(e, cudaMemsetAsync(e->d_row_nan, 0, (size_t)e->rows_padded * sizeof(int), e->stream));
+    MDSX_CUDA(e, cudaMallocHost(&e->h_out, 4 * sizeof(double)));
+
+    int rc = make_tmap_2d(e, &e->tmap_delta, e->d_delta, e->delta_f32, e->n, e->n, e->ld, mdsx::kStepCols, rb);
+    if (rc) return rc;
+    for (int b = 0; b < 2; ++b) {
+        rc = make_tmap_2d(e, &e->tmap_x[b], e->d_x[b], e->x_f32, e->n, e->p, e->x_ld, mdsx::kStepCols, e->p);
+        if (rc) return rc;
+    }
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    return MDSX_OK;
+}
+
+// Clears the error word and self-resetting counters after a failed sweep.
+void reset_scratch(mdsx_engine* e) {
+    cudaMemsetAsync(e->d_counts, 0, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned), e->stream);
+    cudaMemsetAsync(e->d_out, 0, 4 * sizeof(double), e->stream);
+    cudaStreamSynchronize(e->stream);
+}
+
+SweepArgs make_args(mdsx_engine* e) {
+    SweepArgs a{};
+    a.n = e->n;
+    a.n_row_blocks = e->n_row_blocks;
+    a.n_chunks = e->n_chunks;
+    a.chunk_steps = e->chunk_steps;
+    a.n_tiles = e->n_tiles;
+    a.rows_padded = e->rows_padded;
+    a.x_ld = e->x_ld;
+    a.x = e->d_x[e->xcur];
+    a.row_nan = e->d_row_nan;
+    const double tau = e->tau, s = std::sqrt(tau);
+    a.tau = tau;
+    a.sqrt_tau = s;
+    // FP32 constants, in terms of d (z = s * d):
+    //   E'   = exp(-tau d^2 / 2) / sqrt(2 pi tau) = 2^(d^2 k_e + log2_k2)
+    //   1/Phi = S(d) / (S(d) - E' P(d)),  S monic cubic, P quadratic
+    a.k_e = (float)(-0.5 * tau * 1.4426950408889634074);
+    a.log2_k2 = (float)std::log2(1.0 / std::sqrt(2.0 * M_PI * tau));
+    a.tp0 = (float)(mdsx::kTailP0 / tau);
+    a.tp1 = (float)(mdsx::kTailP1 / s);
+    a.tp2 = (float)mdsx::kTailP2;
+    a.ts0 = (float)(mdsx::kTailS0 / (s * s * s));
+    a.ts1 = (float)(mdsx::kTailS1 / (s * s));
+    a.ts2 = (float)(mdsx::kTailS2 / s);
+    a.gpart = e->d_gpart;
+    a.lpart = e->d_lpart;
+    a.lrow = e->d_lrow;
+    a.rb_count = e->d_counts;
+    a.done_count = e->d_counts + e->n_row_blocks;
+    a.grad_out = e->d_grad[e->gcur];
+    a.sums_out = e->d_out;
+    a.truncation = e->trunc ? 1 : 0;
+    a.err = reinterpret_cast<int*>(e->d_out + 3);
+    return a;
+}
+
+// Enqueues one fused sweep; does not synchronise.
+int enqueue_sweep(mdsx_engine* e) {
+    if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
+    if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
+    SweepArgs a = make_args(e);
+    MDSX_CUDA(e, mdsx::sweep_launch(e->mode, e->p, e->trunc, e->grid, e->tmap_delta, e->tmap_x[e->xcur], a,
+                                    e->stream));
+    e->last_launches = 1;
+    return MDSX_OK;
+}
+
+// Runs a sweep and brings its sums to the host; both results become known.
+int sweep_and_read(mdsx_engine* e) {
+    int rc = enqueue_sweep(e);
+    if (rc) return rc;
+    MDSX_CUDA(e, cudaMemcpyAsync(e->h_out, e->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    int dev_err = 0;
+    std::memcpy(&dev_err, &e->h_out[3], sizeof(int));
+    if (dev_err != 0) {
+        reset_scratch(e);
+        e->sum_known = e->grad_known = false;
+        return fail(e, MDSX_ETIMEOUT, "a bounded device wait in the sweep kernel timed out");
+    }
+    e->sum_r2 = e->h_out[0];
+    e->sum_log = e->h_out[1];
+    e->sum_known = true;
+    e->grad_known = true;
+    return MDSX_OK;
+}
+
+double sum_of_increments(const mdsx_engine* e) {
+    // src/NewMultiDimensionalScaling.hpp:198-202 with the total halved at :554-557.
+    const double half_r2 = 0.5 * e->sum_r2;
+    if (e->trunc) return 0.5 * e->tau * half_r2 + 0.5 * e->sum_log;
+    return 0.5 * e->tau * half_r2;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mdsx_version(void) { return "mdsx 0.1 (sm_103a)"; }
+
+int mdsx_create(int embedding_dimension, int location_count, long flags, int device, mdsx_engine** out) {
+    if (!out) return fail(nullptr, MDSX_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (embedding_dimension < 1) return fail(nullptr, MDSX_EINVAL, "embeddingDimension must be >= 1");
+    if (embedding_dimension > MDSX_MAX_DIMENSION)
+        return fail(nullptr, MDSX_EUNSUPPORTED, "embeddingDimension above MDSX_MAX_DIMENSION");
+    if (location_count < 1) return fail(nullptr, MDSX_EINVAL, "locationCount must be >= 1");
+    if (location_count > (1 << 20)) return fail(nullptr, MDSX_EINVAL, "locationCount above 2^20");
+    int count = 0;
+    cudaError_t err = cudaGetDeviceCount(&count);
+    if (err != cudaSuccess || count == 0)
+        return fail(nullptr, MDSX_ECUDA, std::string("no CUDA device: ") + cudaGetErrorString(err));
+    if (device < 0) {
+        if (cudaGetDevice(&device) != cudaSuccess) device = 0;
+    }
+    if (device >= count) return fail(nullptr, MDSX_EINVAL, "device index out of range");
+
+    auto* e = new mdsx_engine;
+    e->p = embedding_dimension;
+    e->n = location_count;
+    e->flags = flags;
+    e->device = device;
+    e->trunc = (flags & MDSX_FLAG_LEFT_TRUNCATION) != 0;
+    if (flags & MDSX_FLAG_FLOAT) {
+        e->mode = Mode::kF32;
+        e->delta_f32 = e->x_f32 = true;
+    } else if (flags & MDSX_FLAG_DELTA_F32) {
+        e->mode = Mode::kF64DeltaF32;
+        e->delta_f32 = true;
+    } else {
+        e->mode = Mode::kF64;
+    }
+    DeviceGuard guard(device);
+    int rc = MDSX_OK;
+    if ((err = cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+        rc = cuda_fail(e, err, "cudaDeviceGetAttribute");
+    if (!rc && (err = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        rc = cuda_fail(e, err, "cudaStreamCreate");
+    if (!rc) {
+        e->stream = e->own_stream;
+        rc = plan_and_allocate(e);
+    }
+    if (rc) {
+        g_create_error = e->last_error;
+        free_all(e);
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return MDSX_OK;
+}
+
+int mdsx_destroy(mdsx_engine* e) {
+    if (!e) return MDSX_EINVAL;
+    {
+        DeviceGuard guard(e->device);
+        if (e->stream) cudaStreamSynchronize(e->stream);
+        free_all(e);
+    }
+    delete e;
+    return MDSX_OK;
+}
+
+const char* mdsx_last_error(const mdsx_engine* e) {
+    return e ? e->last_error.c_str() : g_create_error.c_str();
+}
+
+int mdsx_update_locations(mdsx_engine* e, int index, const double* x, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!x) return fail(e, MDSX_EINVAL, "locations pointer is NULL");
+    DeviceGuard guard(e->device);
+    if (index == -1) {
+        if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "updateLocations(-1): length != N*P");
+        MDSX_CUDA(e, cudaMemcpyAsync(e->d_xin, x, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        MDSX_CUDA(e, mdsx::convert_locations(e->d_xin, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+    } else {
+        if (index < 0 || index >= e->n) return fail(e, MDSX_EINVAL, "updateLocations: index out of range");
+        if (length != (size_t)e->p) return fail(e, MDSX_EINVAL, "updateLocations(i): length != P");
+        MDSX_CUDA(e, cudaMemcpyAsync(e->d_xin, x, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        MDSX_CUDA(e, mdsx::set_one_location(e->d_xin, index, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+    }
+    // The host buffer may be reused by the caller as soon as we return.
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    e->sum_known = false;
+    e->grad_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_get_sum_of_increments(mdsx_engine* e, double* out) {
+    if (!e) return MDSX_EINVAL;
+    if (!out) return fail(e, MDSX_EINVAL, "out is NULL");
+    DeviceGuard guard(e->device);
+    if (!e->sum_known) {
+        int rc = sweep_and_read(e);
+        if (rc) return rc;
+    }
+    *out = sum_of_increments(e);
+    return MDSX_OK;
+}
+
+int mdsx_get_log_likelihood_gradient(mdsx_engine* e, double* out, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!out) return fail(e, MDSX_EINVAL, "out is NULL");
+    if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "getLogLikelihoodGradient: length != N*P");
+    DeviceGuard guard(e->device);
+    if (!e->grad_known) {
+        int rc = sweep_and_read(e);
+        if (rc) return rc;
+    }
+    MDSX_CUDA(e, cudaMemcpyAsync(out, e->d_grad[e->gcur], length * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    return MDSX_OK;
+}
+
+int mdsx_store_state(mdsx_engine* e) {
+    if (!e) return MDSX_EINVAL;
+    DeviceGuard guard(e->device);
+    const int other = 1 - e->xcur;
+    const size_t x_bytes = (size_t)e->p * e->x_ld * e->shape.x_elem_bytes;
+    MDSX_CUDA(e, cudaMemcpyAsync(e->d_x[other], e->d_x[e->xcur], x_bytes, cudaMemcpyDeviceToDevice, e->stream));
+    e->stored_grad_known = e->grad_known;
+    if (e->grad_known)
+        MDSX_CUDA(e, cudaMemcpyAsync(e->d_grad[1 - e->gcur], e->d_grad[e->gcur], (size_t)e->n * e->p * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, e->stream));
+    e->stored_sum_r2 = e->sum_r2;
+    e->stored_sum_log = e->sum_log;
+    e->stored_tau = e->tau;
+    return MDSX_OK;
+}
+
+int mdsx_restore_state(mdsx_engine* e) {
+    if (!e) return MDSX_EINVAL;
+    // As the reference: the stored sum comes back and counts as known.
+    e->sum_r2 = e->stored_sum_r2;
+    e->sum_log = e->stored_sum_log;
+    e->sum_known = true;
+    e->tau = e->stored_tau;
+    e->xcur = 1 - e->xcur;
+    e->gcur = 1 - e->gcur;
+    e->grad_known = e->stored_grad_known;
+    return MDSX_OK;
+}
+
+int mdsx_accept_state(mdsx_engine* e) { return e ? MDSX_OK : MDSX_EINVAL; }
+
+int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!data) return fail(e, MDSX_EINVAL, "data pointer is NULL");
+    if (length != (size_t)e->n * e->n) return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N");
+    DeviceGuard guard(e->device);
+    if (!e->delta_f32 && e->ld == e->n) {
+        MDSX_CUDA(e, cudaMemcpyAsync(e->d_delta, data, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    } else {
+        // Stage rows of doubles on the device and convert/pad them in place.
+        const long long chunk_elems = 16LL << 20;  // 128 MB of doubles
+        const long long rows_per_chunk = std::max(1LL, chunk_elems / e->n);
+        double* staging = nullptr;
+        MDSX_CUDA(e, cudaMalloc(&staging, (size_t)std::min<long long>(rows_per_chunk, e->n) * e->n * sizeof(double)));
+        const int elem = e->delta_f32 ? 4 : 8;
+        for (long long r0 = 0; r0 < e->n; r0 += rows_per_chunk) {
+            const long long rows = std::min<long long>(rows_per_chunk, e->n - r0);
+            cudaError_t err = cudaMemcpyAsync(staging, data + r0 * e->n, (size_t)(rows * e->n) * sizeof(double),
+                                              cudaMemcpyHostToDevice, e->stream);
+            if (err == cudaSuccess)
+                err = mdsx::convert_delta_rows(staging, rows, e->n,
+                                               static_cast<char*>(e->d_delta) + (size_t)(r0 * e->ld) * elem, e->ld,
+                                               e->delta_f32, e->stream);
+            if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+            if (err != cudaSuccess) {
+                cudaFree(staging);
+                return cuda_fail(e, err, "setPairwiseData staging");
+            }
+        }
+        cudaFree(staging);
+    }
+    MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, e->delta_f32, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    e->data_set = true;
+    e->sum_known = e->grad_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_set_pairwise_data_f32(mdsx_engine* e, const float* data, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!data) return fail(e, MDSX_EINVAL, "data pointer is NULL");
+    if (length != (size_t)e->n * e->n) return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N");
+    DeviceGuard guard(e->device);
+    if (e->delta_f32) {
+        MDSX_CUDA(e, cudaMemcpy2DAsync(e->d_delta, (size_t)e->ld * sizeof(float), data, (size_t)e->n * sizeof(float),
+                                       (size_t)e->n * sizeof(float), (size_t)e->n, cudaMemcpyHostToDevice, e->stream));
+        MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, true, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+        MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+        e->data_set = true;
+        e->sum_known = e->grad_known = false;
+        return MDSX_OK;
+    }
+    // FP64 storage: widen on the host.
+    std::vector<double> wide(length);
+    for (size_t k = 0; k < length; ++k) wide[k] = (double)data[k];
+    return mdsx_set_pairwise_data(e, wide.data(), length);
+}
+
+int mdsx_set_parameters(mdsx_engine* e, const double* data, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!data) return fail(e, MDSX_EINVAL, "data pointer is NULL");
+    if (length != 1) return fail(e, MDSX_EINVAL, "setParameters: length != 1 (precision only)");
+    if (!(data[0] > 0.0) || !std::isfinite(data[0]))
+        return fail(e, MDSX_EINVAL, "setParameters: precision must be finite and > 0");
+    if (data[0] == e->tau) return MDSX_OK;
+    e->tau = data[0];
+    // The gradient scales with tau; with truncation the sum depends on it too.
+    // (Without truncation the cached sum is kept unscaled, as the reference does.)
+    e->grad_known = false;
+    if (e->trunc) e->sum_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_make_dirty(mdsx_engine* e) {
+    if (!e) return MDSX_EINVAL;
+    e->sum_known = false;
+    e->grad_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_get_internal_dimension(mdsx_engine* e, int* out) {
+    if (!e || !out) return MDSX_EINVAL;
+    *out = e->p;
+    return MDSX_OK;
+}
+
+int mdsx_get_log_likelihood(mdsx_engine* e, double* out) {
+    if (!e) return MDSX_EINVAL;
+    if (!out) return fail(e, MDSX_EINVAL, "out is NULL");
+    double s = 0.0;
+    int rc = mdsx_get_sum_of_increments(e, &s);
+    if (rc) return rc;
+    const double observation_count = (double)e->n * (double)(e->n - 1) / 2.0;
+    *out = 0.5 * (std::log(e->tau) - std::log(2.0 * M_PI)) * observation_count - s;
+    return MDSX_OK;
+}
+
+int mdsx_set_stream(mdsx_engine* e, void* stream) {
+    if (!e) return MDSX_EINVAL;
+    DeviceGuard guard(e->device);
+    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    e->stream = stream ? static_cast<cudaStream_t>(stream) : e->own_stream;
+    return MDSX_OK;
+}
+
+int mdsx_update_locations_device(mdsx_engine* e, const double* d_x, size_t length) {
+    if (!e) return MDSX_EINVAL;
+    if (!d_x) return fail(e, MDSX_EINVAL, "locations pointer is NULL");
+    if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "length != N*P");
+    DeviceGuard guard(e->device);
+    MDSX_CUDA(e, mdsx::convert_locations(d_x, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+    e->sum_known = false;
+    e->grad_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_evaluate_device(mdsx_engine* e, double* d_sum, double* d_gradient) {
+    if (!e) return MDSX_EINVAL;
+    DeviceGuard guard(e->device);
+    int rc = enqueue_sweep(e);
+    if (rc) return rc;
+    int launches = 1;
+    if (d_sum)
+        MDSX_CUDA(e, cudaMemcpyAsync(d_sum, e->d_out + 2, sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+    if (d_gradient)
+        MDSX_CUDA(e, cudaMemcpyAsync(d_gradient, e->d_grad[e->gcur], (size_t)e->n * e->p * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, e->stream));
+    e->last_launches = launches;
+    // Results live on the device; the host-side cache is refreshed lazily.
+    e->sum_known = false;
+    e->grad_known = true;
+    return MDSX_OK;
+}
+
+int mdsx_last_launch_count(mdsx_engine* e, int* out) {
+    if (!e || !out) return MDSX_EINVAL;
+    *out = e->last_launches;
+    return MDSX_OK;
+}
+
+}  // extern "C"
+
+// Dispatch of the three precision modes.
+namespace mdsx {
+bool sweep_shape(Mode mode, int p, KernelShape* out) {
+    switch (mode) {
+        case Mode::kF32: return sweep_shape_f32(p, out);
+        case Mode::kF64: return sweep_shape_f64(p, out);
+        case Mode::kF64DeltaF32: return sweep_shape_f64s32(p, out);
+    }
+    return false;
+}
+cudaError_t sweep_occupancy(Mode mode, int p, bool trunc, int* ctas) {
+    switch (mode) {
+        case Mode::kF32: return sweep_occupancy_f32(p, trunc, ctas);
+        case Mode::kF64: return sweep_occupancy_f64(p, trunc, ctas);
+        case Mode::kF64DeltaF32: return sweep_occupancy_f64s32(p, trunc, ctas);
+    }
+    return cudaErrorInvalidValue;
+}
+cudaError_t sweep_launch(Mode mode, int p, bool trunc, int grid, const CUtensorMap& td, const CUtensorMap& tx,
+                         const SweepArgs& args, cudaStream_t stream) {
+    switch (mode) {
+        case Mode::kF32: return sweep_launch_f32(p, trunc, grid, td, tx, args, stream);
+        case Mode::kF64: return sweep_launch_f64(p, trunc, grid, td, tx, args, stream);
+        case Mode::kF64DeltaF32: return sweep_launch_f64s32(p, trunc, grid, td, tx, args, stream);
+    }
+    return cudaErrorInvalidValue;
+}
+}  // namespace mdsx

@@ -1,0 +1,124 @@
+// Layout kernels: locations into the SoA compute layout, delta rows into the
+// padded storage layout (the NaN-preserving double -> float conversion of
+// src/MemoryManagement.hpp:45-56 in MassiveMDS), and the per-row NaN marks the
+// sweep uses to pick its masked path.
+#include <cstdint>
+
+#include "sweep.h"
+
+namespace mdsx {
+namespace {
+
+template <typename C>
+__global__ void convert_locations_kernel(const double* __restrict__ src, int n, int p, C* __restrict__ dst, int x_ld) {
+    const long long total = (long long)p * x_ld;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(idx / x_ld);
+        const int i = (int)(idx - (long long)q * x_ld);
+        dst[idx] = i < n ? (C)src[(long long)i * p + q] : C(0);
+    }
+}
+
+template <typename C>
+__global__ void set_one_location_kernel(const double* __restrict__ src, int index, int p, C* __restrict__ dst,
+                                        int x_ld) {
+    const int q = threadIdx.x;
+    if (q < p) dst[(long long)q * x_ld + index] = (C)src[q];
+}
+
+template <typename T>
+__global__ void convert_delta_rows_kernel(const double* __restrict__ src, long long rows, int n, T* __restrict__ dst,
+                                          long long ld) {
+    const long long total = rows * n;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long r = idx / n;
+        const long long c = idx - r * n;
+        dst[r * ld + c] = (T)src[idx];  // NaN converts to NaN
+    }
+}
+
+__global__ void copy_delta_rows_f32_kernel(const float* __restrict__ src, long long rows, int n, float* __restrict__ dst,
+                                           long long ld) {
+    const long long total = rows * n;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long r = idx / n;
+        const long long c = idx - r * n;
+        dst[r * ld + c] = src[idx];
+    }
+}
+
+// One warp per row.
+template <typename T>
+__global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int n, long long ld, int* __restrict__ row_nan,
+                                     int rows_padded) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < rows_padded; row += warps) {
+        int bad = 0;
+        if (row < n) {
+            const T* r = delta + (long long)row * ld;
+            for (int c = lane; c < n; c += 32) bad |= (r[c] != r[c]);
+            bad = __any_sync(0xffffffffu, bad);
+        } else {
+            bad = 1;
+        }
+        if (lane == 0) row_nan[row] = bad;
+    }
+}
+
+int grid_for(long long work, int threads) {
+    long long blocks = (work + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 4096) blocks = 4096;
+    return (int)blocks;
+}
+
+}  // namespace
+
+cudaError_t convert_locations(const double* src, int n, int p, void* dst, int x_ld, bool to_f32, cudaStream_t s) {
+    const int grid = grid_for((long long)p * x_ld, 256);
+    if (to_f32)
+        convert_locations_kernel<float><<<grid, 256, 0, s>>>(src, n, p, static_cast<float*>(dst), x_ld);
+    else
+        convert_locations_kernel<double><<<grid, 256, 0, s>>>(src, n, p, static_cast<double*>(dst), x_ld);
+    return cudaGetLastError();
+}
+
+cudaError_t set_one_location(const double* src, int index, int p, void* dst, int x_ld, bool to_f32, cudaStream_t s) {
+    if (to_f32)
+        set_one_location_kernel<float><<<1, 32, 0, s>>>(src, index, p, static_cast<float*>(dst), x_ld);
+    else
+        set_one_location_kernel<double><<<1, 32, 0, s>>>(src, index, p, static_cast<double*>(dst), x_ld);
+    return cudaGetLastError();
+}
+
+cudaError_t convert_delta_rows(const double* src, long long rows, int n, void* dst, long long ld, bool to_f32,
+                               cudaStream_t s) {
+    const int grid = grid_for(rows * n, 256);
+    if (to_f32)
+        convert_delta_rows_kernel<float><<<grid, 256, 0, s>>>(src, rows, n, static_cast<float*>(dst), ld);
+    else
+        convert_delta_rows_kernel<double><<<grid, 256, 0, s>>>(src, rows, n, static_cast<double*>(dst), ld);
+    return cudaGetLastError();
+}
+
+cudaError_t copy_delta_rows_f32(const float* src, long long rows, int n, float* dst, long long ld, cudaStream_t s) {
+    copy_delta_rows_f32_kernel<<<grid_for(rows * n, 256), 256, 0, s>>>(src, rows, n, dst, ld);
+    return cudaGetLastError();
+}
+
+cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, int* row_nan, int rows_padded,
+                          cudaStream_t s) {
+    const int grid = grid_for((long long)rows_padded * 32, 256);
+    if (is_f32)
+        mark_nan_rows_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(delta), n, ld, row_nan, rows_padded);
+    else
+        mark_nan_rows_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(delta), n, ld, row_nan,
+                                                          rows_padded);
+    return cudaGetLastError();
+}
+
+}  // namespace mdsx

@@ -1,0 +1,4 @@
+// Sweep kernel instances: FP32 pair arithmetic over FP32-stored delta (P = 1..10, truncation on/off).
+#include "sweep_dispatch.cuh"
+
+MDSX_DEFINE_MODE(f32, float, float)

@@ -1,0 +1,326 @@
+"""GPU parity tests: the CUDA engine, called through the C ABI, against the
+reference engine's golden vectors and the FP64 oracle.
+
+Tolerances (from the engine's stated targets):
+  FP64 mode (and FP64 over FP32-stored delta): sum of increments within 1e-10
+    relative, gradient within 1e-9 norm-relative (max |dg| / max |g|).
+  FP32 mode (FP32 pairs, compensated FP32 partials, FP64 reductions): within
+    1e-5 relative of the FP64 oracle on the same (FP32-rounded) delta.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from massivemds_gb300 import Engine, MdsxError, flags as F
+from massivemds_gb300 import data as gen
+
+pytestmark = pytest.mark.gpu
+
+TOL_F64_SUM, TOL_F64_GRAD = 1e-10, 1e-9
+TOL_F32 = 1e-5
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def grad_rel(g, ref):
+    g = np.asarray(g).reshape(ref.shape)
+    return np.abs(g - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+def make_engine(n, p, trunc, mode, delta, x, tau):
+    fl = F.LEFT_TRUNCATION if trunc else 0
+    fl |= {"f64": 0, "f32": F.FLOAT, "f64s32": F.DELTA_F32}[mode]
+    e = Engine(p, n, fl)
+    e.setPairwiseData(delta)
+    e.updateLocations(-1, x)
+    e.setParameters([tau])
+    e.makeDirty()
+    return e
+
+
+def oracle_delta(delta, mode):
+    return delta.astype(np.float32) if mode in ("f32", "f64s32") else delta
+
+
+def tolerances(mode):
+    return (TOL_F32, TOL_F32) if mode == "f32" else (TOL_F64_SUM, TOL_F64_GRAD)
+
+
+# ------------------------------------------------------------- golden vectors
+
+def test_fp64_matches_reference_golden(golden):
+    data, cases = golden
+    for name in cases:
+        n, p, trunc, tau, use_float = data[f"{name}.meta"]
+        if use_float:
+            continue
+        n, p = int(n), int(p)
+        e = make_engine(n, p, bool(trunc), "f64", data[f"{name}.delta"], data[f"{name}.x"], tau)
+        s = e.getSumOfIncrements()
+        g = e.getLogLikelihoodGradient()
+        e.close()
+        ref_g = data[f"{name}.grad"].reshape(n, p)
+        assert rel(s, float(data[f"{name}.sum"])) < TOL_F64_SUM, name
+        assert grad_rel(g, ref_g) < TOL_F64_GRAD, name
+
+
+def test_fp32_matches_oracle_on_golden_inputs(golden):
+    data, cases = golden
+    for name in cases:
+        n, p, trunc, tau, _ = data[f"{name}.meta"]
+        n, p = int(n), int(p)
+        delta, x = data[f"{name}.delta"], data[f"{name}.x"]
+        e = make_engine(n, p, bool(trunc), "f32", delta, x, tau)
+        s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+        e.close()
+        d32 = delta.astype(np.float32)
+        assert rel(s, oracle.sum_of_increments(d32, x, tau, bool(trunc))) < TOL_F32, name
+        assert grad_rel(g, oracle.gradient(d32, x, tau, bool(trunc))) < TOL_F32, name
+
+
+def test_reference_call_sequence_golden(golden):
+    """The reference benchmark's store/update/sum/restore-or-accept/gradient loop
+    (src/benchmark.cpp:250-309) gives the reference engine's sums and gradients."""
+    data, _ = golden
+    delta, x0, tau = data["seq.delta"], data["seq.x0"], float(data["seq.tau"])
+    n, p = x0.shape
+    for mode in ("f64", "f32"):
+        tol_s, tol_g = tolerances(mode)
+        e = make_engine(n, p, True, mode, delta, x0, tau)
+        assert rel(e.getSumOfIncrements(), data["seq.sums"][0]) < tol_s
+        for k, (xn, restore) in enumerate(zip(data["seq.xs"], data["seq.restores"])):
+            e.storeState()
+            e.updateLocations(-1, xn)
+            assert rel(e.getSumOfIncrements(), data["seq.sums"][k + 1]) < tol_s, (mode, k)
+            if restore:
+                e.restoreState()
+            else:
+                e.acceptState()
+            assert grad_rel(e.getLogLikelihoodGradient(), data["seq.grads"][k + 1]) < tol_g, (mode, k)
+        e.close()
+
+
+# ----------------------------------------------------------- random coverage
+
+def _inputs(n, p, seed, nans=0, asym=False):
+    rng = np.random.default_rng(seed)
+    y = rng.standard_normal((n, 6))
+    delta = np.sqrt(((y[:, None] - y[None]) ** 2).sum(-1))
+    if asym:
+        delta = delta * (1.0 + 0.1 * rng.random((n, n)))
+        np.fill_diagonal(delta, 0.0)
+    for _ in range(nans):
+        i, j = rng.choice(n, 2, replace=False)
+        delta[i, j] = np.nan
+    return delta, rng.standard_normal((n, p))
+
+
+@pytest.mark.parametrize("mode", ["f64", "f32", "f64s32"])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 31, 32, 33, 127, 128, 129, 257, 1000])
+def test_sizes_and_edges(mode, n):
+    p, tau = 2, 1.7
+    delta, x = _inputs(n, p, seed=n, nans=min(3, n // 10))
+    tol_s, tol_g = tolerances(mode)
+    for trunc in (True, False):
+        e = make_engine(n, p, trunc, mode, delta, x, tau)
+        s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+        e.close()
+        od = oracle_delta(delta, mode)
+        s_ref = oracle.sum_of_increments(od, x, tau, trunc)
+        g_ref = oracle.gradient(od, x, tau, trunc)
+        if n == 1:
+            assert s == 0.0 and np.all(g == 0.0)
+            continue
+        assert rel(s, s_ref) < tol_s, (trunc, s, s_ref)
+        assert grad_rel(g, g_ref) < tol_g, trunc
+
+
+@pytest.mark.parametrize("mode", ["f64", "f32"])
+@pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
+def test_dimensions(mode, p):
+    n, tau = 300, 0.8
+    delta, x = _inputs(n, p, seed=100 + p, nans=2, asym=True)
+    tol_s, tol_g = tolerances(mode)
+    for trunc in (True, False):
+        e = make_engine(n, p, trunc, mode, delta, x, tau)
+        s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+        e.close()
+        od = oracle_delta(delta, mode)
+        assert rel(s, oracle.sum_of_increments(od, x, tau, trunc)) < tol_s
+        assert grad_rel(g, oracle.gradient(od, x, tau, trunc)) < tol_g
+
+
+def test_nan_rows_and_asymmetric_delta():
+    n, p, tau = 400, 2, 2.0
+    delta, x = _inputs(n, p, seed=7, nans=0, asym=True)
+    delta[5, :] = np.nan       # a whole row missing
+    delta[:, 9] = np.nan       # a whole column missing
+    delta[100, 101] = np.nan
+    for mode in ("f64", "f32"):
+        tol_s, tol_g = tolerances(mode)
+        e = make_engine(n, p, True, mode, delta, x, tau)
+        s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+        e.close()
+        od = oracle_delta(delta, mode)
+        assert rel(s, oracle.sum_of_increments(od, x, tau)) < tol_s
+        gr = oracle.gradient(od, x, tau)
+        assert grad_rel(g, gr) < tol_g
+        assert np.all(np.asarray(g).reshape(n, p)[5] == 0.0)  # row 5 has no observed pair
+
+
+def test_precision_extremes():
+    n, p = 500, 2
+    delta, x = _inputs(n, p, seed=9)
+    for tau in (1e-3, 0.05, 40.0, 900.0):
+        for mode in ("f64", "f32"):
+            tol_s, tol_g = tolerances(mode)
+            e = make_engine(n, p, True, mode, delta, x, tau)
+            s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+            e.close()
+            od = oracle_delta(delta, mode)
+            assert rel(s, oracle.sum_of_increments(od, x, tau)) < tol_s, (mode, tau)
+            assert grad_rel(g, oracle.gradient(od, x, tau)) < tol_g, (mode, tau)
+
+
+# ------------------------------------------------------------ state machine
+
+def test_single_location_update_and_caching():
+    n, p, tau = 200, 3, 1.2
+    delta, x = _inputs(n, p, seed=11)
+    e = make_engine(n, p, True, "f64", delta, x, tau)
+    s0 = e.getSumOfIncrements()
+    x2 = x.copy()
+    x2[17] = [0.3, -0.2, 1.1]
+    e.updateLocations(17, x2[17])
+    s1 = e.getSumOfIncrements()
+    assert rel(s1, oracle.sum_of_increments(delta, x2, tau)) < TOL_F64_SUM
+    assert s1 != s0
+    g = e.getLogLikelihoodGradient()
+    assert grad_rel(g, oracle.gradient(delta, x2, tau)) < TOL_F64_GRAD
+    # setParameters invalidates; untruncated sums rescale with the new precision
+    e.setParameters([2.4])
+    assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta, x2, 2.4)) < TOL_F64_SUM
+    e.close()
+    e = make_engine(n, p, False, "f64", delta, x, tau)
+    e.getSumOfIncrements()
+    e.setParameters([3.3])
+    assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta, x, 3.3, False)) < TOL_F64_SUM
+    assert grad_rel(e.getLogLikelihoodGradient(), oracle.gradient(delta, x, 3.3, False)) < TOL_F64_GRAD
+    assert e.getInternalDimension() == p
+    e.close()
+
+
+def test_restore_returns_stored_sum_without_sweep():
+    """restoreState brings back the stored sum as known (src/NewMultiDimensionalScaling.hpp:234-236)."""
+    n, p, tau = 100, 2, 1.0
+    delta, x = _inputs(n, p, seed=12)
+    e = make_engine(n, p, True, "f64", delta, x, tau)
+    s0 = e.getSumOfIncrements()
+    g0 = e.getLogLikelihoodGradient().copy()
+    e.storeState()
+    e.updateLocations(-1, x + 0.5)
+    assert e.getSumOfIncrements() != s0
+    e.restoreState()
+    assert e.getSumOfIncrements() == s0
+    assert np.array_equal(e.getLogLikelihoodGradient(), g0)
+    e.close()
+
+
+def test_deterministic_bitwise():
+    n, p, tau = 3000, 2, 2.0
+    delta, x = _inputs(n, p, seed=13)
+    for mode in ("f32", "f64"):
+        e = make_engine(n, p, True, mode, delta, x, tau)
+        s1, g1 = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
+        e.makeDirty()
+        s2, g2 = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
+        e.close()
+        assert s1 == s2 and np.array_equal(g1, g2), mode
+
+
+def test_log_likelihood_assembly():
+    n, p, tau = 150, 2, 1.4
+    delta, x = _inputs(n, p, seed=14)
+    e = make_engine(n, p, True, "f64", delta, x, tau)
+    ll = e.getLogLikelihood()
+    s = oracle.sum_of_increments(delta, x, tau)
+    assert rel(ll, oracle.log_likelihood(s, n, tau)) < TOL_F64_SUM
+    e.close()
+
+
+# ------------------------------------------------------------------- errors
+
+def test_error_statuses():
+    n, p = 50, 2
+    delta, x = _inputs(n, p, seed=15)
+    e = Engine(p, n, F.LEFT_TRUNCATION)
+    with pytest.raises(MdsxError) as err:
+        e.getSumOfIncrements()
+    assert err.value.status == 5  # ESTATE: no data yet
+    with pytest.raises(MdsxError) as err:
+        e.setPairwiseData(delta[:-1])
+    assert err.value.status == 1
+    e.setPairwiseData(delta)
+    with pytest.raises(MdsxError) as err:
+        e.updateLocations(-1, x[:-1])
+    assert err.value.status == 1
+    with pytest.raises(MdsxError):
+        e.updateLocations(n, x[0])
+    with pytest.raises(MdsxError):
+        e.setParameters([-1.0])
+    with pytest.raises(MdsxError):
+        e.setParameters([1.0, 2.0])
+    e.updateLocations(-1, x)
+    with pytest.raises(MdsxError) as err:
+        e.getSumOfIncrements()
+    assert err.value.status == 5  # precision not set
+    e.setParameters([1.0])
+    assert np.isfinite(e.getSumOfIncrements())
+    with pytest.raises(ValueError):
+        e.getLogLikelihoodGradient(np.empty(3))
+    e.close()
+
+
+# ------------------------------------------------------- device-resident API
+
+def test_device_api_matches_host_api():
+    torch = pytest.importorskip("torch")
+    n, p, tau = 700, 2, 2.0
+    delta, x = _inputs(n, p, seed=16)
+    for mode in ("f32", "f64"):
+        e = make_engine(n, p, True, mode, delta, x, tau)
+        s_host, g_host = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
+        dx = torch.tensor(x, dtype=torch.float64, device="cuda")
+        dsum = torch.zeros(1, dtype=torch.float64, device="cuda")
+        dgrad = torch.zeros(n * p, dtype=torch.float64, device="cuda")
+        stream = torch.cuda.Stream()
+        e.set_stream(stream.cuda_stream)
+        e.update_locations_device(dx.data_ptr())
+        e.evaluate_device(dsum.data_ptr(), dgrad.data_ptr())
+        stream.synchronize()
+        assert e.last_launch_count() >= 1
+        assert float(dsum.item()) == s_host
+        assert np.array_equal(dgrad.cpu().numpy(), g_host)
+        e.set_stream(None)
+        e.close()
+
+
+# ------------------------------------------------------------ full size (N=20k)
+
+@pytest.mark.parametrize("mode", ["f32", "f64s32"])
+def test_full_size_n20000(mode):
+    """The N=20 000, P=2, tau=2 workload with FP32-stored delta: one evaluation
+    against the FP64 oracle on the same FP32 delta."""
+    n, p, tau = 20000, 2, 2.0
+    delta = gen.noisy_delta(n, dim=10, noise_sd=0.05, seed=666, dtype=np.float32)
+    x = gen.locations(n, p, seed=667)
+    tol_s, tol_g = tolerances(mode)
+    e = make_engine(n, p, True, mode, delta, x, tau)
+    s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+    e.close()
+    s_ref = oracle.sum_of_increments(delta, x, tau)
+    assert rel(s, s_ref) < tol_s
+    g_full = oracle.gradient(delta, x, tau)
+    assert grad_rel(g, g_full) < tol_g
