@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,7 +46,8 @@ struct mdsx_engine {
     int sm_count = 0;
 
     KernelShape shape{};
-    int n_row_blocks = 0, rows_padded = 0, chunk_steps = 0, n_chunks = 0, n_tiles = 0, grid = 0;
+    int n_row_blocks = 0, rows_padded = 0, steps_per_row = 0, grid = 0, max_slots = 0;
+    long long n_units = 0;
 
     void* d_delta = nullptr;
     long long ld = 0;
@@ -173,17 +175,18 @@ int plan_and_allocate(mdsx_engine* e) {
     const int rb = e->shape.rb;
     e->n_row_blocks = (e->n + rb - 1) / rb;
     e->rows_padded = e->n_row_blocks * rb;
-    const int steps_total = (e->n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+    // Stream-K partition: U = row blocks x 128-column stages, split evenly
+    // over G <= U CTAs (so no CTA has an empty range).
+    e->steps_per_row = (e->n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+    e->n_units = (long long)e->n_row_blocks * e->steps_per_row;
     const long long grid_max = (long long)e->sm_count * ctas;
-    // About 16 tiles per resident CTA, so the static round-robin tile order
-    // balances to within a few percent.
-    const long long target_tiles = 16 * grid_max;
-    long long chunks = (target_tiles + e->n_row_blocks - 1) / e->n_row_blocks;
-    chunks = std::max(1LL, std::min<long long>(chunks, steps_total));
-    e->chunk_steps = (int)((steps_total + chunks - 1) / chunks);
-    e->n_chunks = (steps_total + e->chunk_steps - 1) / e->chunk_steps;
-    e->n_tiles = e->n_row_blocks * e->n_chunks;
-    e->grid = (int)std::min<long long>(e->n_tiles, grid_max);
+    e->grid = (int)std::min<long long>(e->n_units, grid_max);
+    e->max_slots = 1;
+    for (int rb = 0; rb < e->n_row_blocks; ++rb) {
+        const long long u0 = (long long)rb * e->steps_per_row, u1 = u0 + e->steps_per_row - 1;
+        const int slots = mdsx::cta_of_unit(u1, e->n_units, e->grid) - mdsx::cta_of_unit(u0, e->n_units, e->grid) + 1;
+        e->max_slots = std::max(e->max_slots, slots);
+    }
 
     const int delta_elem = e->shape.delta_elem_bytes;
     e->ld = round_up(e->n, 16 / delta_elem);
@@ -201,8 +204,9 @@ int plan_and_allocate(mdsx_engine* e) {
     MDSX_CUDA(e, cudaMalloc(&e->d_grad[1], (size_t)e->n * e->p * sizeof(double)));
     MDSX_CUDA(e, cudaMalloc(&e->d_out, 4 * sizeof(double)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_out, 0, 4 * sizeof(double), e->stream));
-    MDSX_CUDA(e, cudaMalloc(&e->d_gpart, (size_t)e->n_chunks * e->rows_padded * e->p * acc_bytes));
-    MDSX_CUDA(e, cudaMalloc(&e->d_lpart, (size_t)e->n_tiles * mdsx::kConsumerWarps * 2 * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_gpart, (size_t)e->n_row_blocks * e->max_slots * rb * e->p * acc_bytes));
+    MDSX_CUDA(e, cudaMalloc(&e->d_lpart,
+                            (size_t)e->n_row_blocks * e->max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
     MDSX_CUDA(e, cudaMalloc(&e->d_lrow, (size_t)e->n_row_blocks * 2 * sizeof(double)));
     MDSX_CUDA(e, cudaMalloc(&e->d_counts, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_counts, 0, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned), e->stream));
@@ -231,9 +235,10 @@ SweepArgs make_args(mdsx_engine* e) {
     SweepArgs a{};
     a.n = e->n;
     a.n_row_blocks = e->n_row_blocks;
-    a.n_chunks = e->n_chunks;
-    a.chunk_steps = e->chunk_steps;
-    a.n_tiles = e->n_tiles;
+    a.steps_per_row = e->steps_per_row;
+    a.grid = e->grid;
+    a.n_units = e->n_units;
+    a.max_slots = e->max_slots;
     a.rows_padded = e->rows_padded;
     a.x_ld = e->x_ld;
     a.x = e->d_x[e->xcur];
