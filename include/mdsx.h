@@ -135,6 +135,33 @@ int mdsx_evaluate_device(mdsx_engine* engine, double* d_sum, double* d_gradient)
 /* Number of kernel launches the last sweep issued (for launch accounting). */
 int mdsx_last_launch_count(mdsx_engine* engine, int* out);
 
+/* ---- Allocation-free variant (no counterpart in the reference) ----
+ * For callers that cannot allocate device memory: hosts whose GPU memory is
+ * owned by another allocator (a JVM or R process sharing the device with a
+ * framework that has reserved it) and sampler loops that must not call
+ * cudaMalloc/cudaFree, which can fail at run time and synchronise the device.
+ *
+ * One fused FP32 sweep (the MDSX_FLAG_FLOAT arithmetic) over caller-owned
+ * device buffers: d_delta is N x N float, row stride delta_ld floats (a
+ * multiple of 4, >= N, 16-byte aligned base; NaN = missing); d_locations is
+ * N*P row-major doubles; writes getSumOfIncrements() to *d_sum_of_increments
+ * and the N*P gradient to d_gradient (device doubles). Synchronous on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream).
+ *
+ * All scratch lives in one static device array of MDSX_NOALLOC_SCRATCH_BYTES,
+ * held on every GPU that loads the library until the process exits. The first
+ * call on a device resolves that array's address (cudaGetSymbolAddress), so
+ * make it before any stream capture. Calls share the array: calls that overlap
+ * on the GPU race and must be serialised. Problems whose scratch does not fit
+ * (N above MDSX_NOALLOC_MAX_LOCATIONS, or a plan too large) return MDSX_EINVAL;
+ * mdsx_last_error(NULL) then gives the message. No cudaMalloc, cudaFree or
+ * allocating library routine is called. */
+#define MDSX_NOALLOC_SCRATCH_BYTES (8u << 20)
+#define MDSX_NOALLOC_MAX_LOCATIONS 32768
+int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const double* d_locations,
+                           int location_count, int embedding_dimension, double precision, int truncation,
+                           double* d_sum_of_increments, double* d_gradient, void* stream);
+
 /* Library version string. */
 const char* mdsx_version(void);
 

@@ -601,6 +601,8 @@ int mdsx_last_launch_count(mdsx_engine* e, int* out) {
 
 // Dispatch of the three precision modes.
 namespace mdsx {
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+
 bool sweep_shape(Mode mode, int p, KernelShape* out) {
     switch (mode) {
         case Mode::kF32: return sweep_shape_f32(p, out);

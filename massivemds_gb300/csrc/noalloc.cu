@@ -1,0 +1,222 @@
+// Allocation-free entry point: the FP32 fused sweep with its scratch in a
+// file-scope device array instead of cudaMalloc'd buffers.
+//
+// Who needs it: callers that must not allocate device memory themselves or
+// through this library -- hosts whose GPU memory is owned by another
+// allocator (a JVM or R process sharing the device with a framework that has
+// reserved it), and sampler loops that cannot afford cudaMalloc/cudaFree in
+// their inner loop (both can fail at run time and synchronise the device).
+// They pass device buffers for delta, the locations and both outputs; every
+// intermediate lives in g_noalloc_scratch below.
+//
+// Rules of use:
+//  - Every GPU that loads libmdsx.so holds kNoAllocScratchBytes of device
+//    memory for this array until the process exits.
+//  - The first call on a device resolves the array's device address with
+//    cudaGetSymbolAddress (once per device, with that device current). Make
+//    that first call before any stream capture.
+//  - All calls share the one array and it keeps the previous call's contents;
+//    each call clears the counters and the error word it needs at zero. Calls
+//    whose work overlaps on the GPU (other streams, other host threads) race
+//    on the scratch: serialise them.
+//  - Sizes whose scratch does not fit are rejected with MDSX_EINVAL.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/mdsx.h"
+#include "normal_rational.h"
+#include "sweep.h"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = MDSX_NOALLOC_SCRATCH_BYTES;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+void* g_scratch_ptr[kMaxDevices] = {};
+int noalloc_fail(int code, const std::string& msg) {
+    mdsx::set_global_error(msg);  // read back with mdsx_last_error(NULL)
+    return code;
+}
+
+int noalloc_cuda_fail(cudaError_t err, const char* what) {
+    return noalloc_fail(MDSX_ECUDA, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+#define NOALLOC_CUDA(call)                                      \
+    do {                                                        \
+        cudaError_t _err = (call);                              \
+        if (_err != cudaSuccess) return noalloc_cuda_fail(_err, #call); \
+    } while (0)
+
+// Device address of g_noalloc_scratch on the current device (resolved once).
+int scratch_address(int device, void** out) {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_ptr[device]) {
+        void* ptr = nullptr;
+        cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (err != cudaSuccess) return noalloc_cuda_fail(err, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_scratch_ptr[device] = ptr;
+    }
+    *out = g_scratch_ptr[device];
+    return MDSX_OK;
+}
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
+
+int tmap_f32(CUtensorMap* map, const void* base, long long cols, long long rows, long long ld, unsigned box_cols,
+             unsigned box_rows) {
+    auto fn = encode_tiled();
+    if (!fn) return noalloc_fail(MDSX_ECUDA, "cuTensorMapEncodeTiled unavailable from the driver");
+    cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)(ld * 4)};
+    cuuint32_t box[2] = {box_cols, box_rows};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), gdim, gstride, box, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return noalloc_fail(MDSX_ECUDA, "cuTensorMapEncodeTiled failed");
+    return MDSX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const double* d_locations, int location_count,
+                           int embedding_dimension, double precision, int truncation, double* d_sum_of_increments,
+                           double* d_gradient, void* stream_handle) {
+    const int n = location_count, p = embedding_dimension;
+    if (!d_delta || !d_locations || !d_sum_of_increments || !d_gradient)
+        return noalloc_fail(MDSX_EINVAL, "a device pointer is NULL");
+    if (p < 1 || p > MDSX_MAX_DIMENSION) return noalloc_fail(MDSX_EINVAL, "embeddingDimension outside 1..MDSX_MAX_DIMENSION");
+    if (n < 1) return noalloc_fail(MDSX_EINVAL, "locationCount must be >= 1");
+    if (n > MDSX_NOALLOC_MAX_LOCATIONS)
+        return noalloc_fail(MDSX_EINVAL, "locationCount above MDSX_NOALLOC_MAX_LOCATIONS for the allocation-free sweep");
+    if (delta_ld < n || delta_ld % 4 != 0)
+        return noalloc_fail(MDSX_EINVAL, "delta_ld must be >= locationCount and a multiple of 4 floats");
+    if (reinterpret_cast<uintptr_t>(d_delta) % 16 != 0) return noalloc_fail(MDSX_EINVAL, "delta must be 16-byte aligned");
+    if (!(precision > 0.0) || !std::isfinite(precision)) return noalloc_fail(MDSX_EINVAL, "precision must be finite and > 0");
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_handle);
+
+    int device = 0;
+    NOALLOC_CUDA(cudaGetDevice(&device));
+    if (device >= kMaxDevices) return noalloc_fail(MDSX_EINVAL, "device index above the supported count");
+    void* base = nullptr;
+    int rc = scratch_address(device, &base);
+    if (rc) return rc;
+
+    // Same tile plan as the engine's FP32 mode.
+    mdsx::KernelShape shape{};
+    if (!mdsx::sweep_shape(mdsx::Mode::kF32, p, &shape)) return noalloc_fail(MDSX_EUNSUPPORTED, "dimension not built");
+    int ctas = 0, sms = 0;
+    NOALLOC_CUDA(mdsx::sweep_occupancy(mdsx::Mode::kF32, p, truncation != 0, &ctas));
+    NOALLOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int rb = shape.rb;
+    const int n_row_blocks = (n + rb - 1) / rb;
+    const int rows_padded = n_row_blocks * rb;
+    const int steps_per_row = (n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+    const long long n_units = (long long)n_row_blocks * steps_per_row;
+    const int grid = (int)std::min<long long>(n_units, (long long)sms * std::max(ctas, 1));
+    int max_slots = 1;
+    for (int b = 0; b < n_row_blocks; ++b) {
+        const long long u0 = (long long)b * steps_per_row, u1 = u0 + steps_per_row - 1;
+        max_slots = std::max(max_slots, mdsx::cta_of_unit(u1, n_units, grid) - mdsx::cta_of_unit(u0, n_units, grid) + 1);
+    }
+    const int x_ld = (int)std::max<long long>((n + mdsx::kStepCols - 1) / mdsx::kStepCols * mdsx::kStepCols, rows_padded);
+
+    // Carve the scratch: [out: 4 doubles][counters][row marks][x SoA][gpart][lpart][lrow]
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = off;
+        off = align256(off + bytes);
+        return static_cast<unsigned char*>(base) + at;
+    };
+    double* out = reinterpret_cast<double*>(take(4 * sizeof(double)));
+    unsigned* counts = reinterpret_cast<unsigned*>(take(((size_t)n_row_blocks + 1) * sizeof(unsigned)));
+    int* row_nan = reinterpret_cast<int*>(take((size_t)rows_padded * sizeof(int)));
+    float* x = reinterpret_cast<float*>(take((size_t)p * x_ld * sizeof(float)));
+    float* gpart = reinterpret_cast<float*>(take((size_t)n_row_blocks * max_slots * rb * p * sizeof(float)));
+    double* lpart =
+        reinterpret_cast<double*>(take((size_t)n_row_blocks * max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
+    double* lrow = reinterpret_cast<double*>(take((size_t)n_row_blocks * 2 * sizeof(double)));
+    if (off > kNoAllocScratchBytes)
+        return noalloc_fail(MDSX_EINVAL, "problem needs " + std::to_string(off) + " bytes of scratch; the allocation-free "
+                            "sweep has " + std::to_string(kNoAllocScratchBytes));
+
+    // Counters, sums and the error word must start at zero.
+    NOALLOC_CUDA(cudaMemsetAsync(out, 0, 4 * sizeof(double), stream));
+    NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
+    NOALLOC_CUDA(mdsx::convert_locations(d_locations, n, p, x, x_ld, true, stream));
+    NOALLOC_CUDA(mdsx::mark_nan_rows(d_delta, true, n, delta_ld, row_nan, rows_padded, stream));
+
+    CUtensorMap tmap_delta{}, tmap_x{};
+    rc = tmap_f32(&tmap_delta, d_delta, n, n, delta_ld, mdsx::kStepCols, rb);
+    if (rc) return rc;
+    rc = tmap_f32(&tmap_x, x, n, p, x_ld, mdsx::kStepCols, p);
+    if (rc) return rc;
+
+    mdsx::SweepArgs a{};
+    a.n = n;
+    a.n_row_blocks = n_row_blocks;
+    a.steps_per_row = steps_per_row;
+    a.grid = grid;
+    a.n_units = n_units;
+    a.max_slots = max_slots;
+    a.rows_padded = rows_padded;
+    a.x_ld = x_ld;
+    a.x = x;
+    a.row_nan = row_nan;
+    const double tau = precision, s = std::sqrt(tau);
+    a.tau = tau;
+    a.sqrt_tau = s;
+    a.k_e = (float)(-0.5 * tau * 1.4426950408889634074);
+    a.log2_k2 = (float)std::log2(1.0 / std::sqrt(2.0 * M_PI * tau));
+    a.tp0 = (float)(mdsx::kTailP0 / tau);
+    a.tp1 = (float)(mdsx::kTailP1 / s);
+    a.tp2 = (float)mdsx::kTailP2;
+    a.ts0 = (float)(mdsx::kTailS0 / (s * s * s));
+    a.ts1 = (float)(mdsx::kTailS1 / (s * s));
+    a.ts2 = (float)(mdsx::kTailS2 / s);
+    a.gpart = gpart;
+    a.lpart = lpart;
+    a.lrow = lrow;
+    a.rb_count = counts;
+    a.done_count = counts + n_row_blocks;
+    a.grad_out = d_gradient;
+    a.sums_out = out;
+    a.truncation = truncation ? 1 : 0;
+    a.err = reinterpret_cast<int*>(out + 3);
+    NOALLOC_CUDA(mdsx::sweep_launch(mdsx::Mode::kF32, p, truncation != 0, grid, tmap_delta, tmap_x, a, stream));
+    NOALLOC_CUDA(cudaMemcpyAsync(d_sum_of_increments, out + 2, sizeof(double), cudaMemcpyDeviceToDevice, stream));
+
+    // Synchronous like the rest of the ABI: report a device-side timeout.
+    int dev_err = 0;
+    NOALLOC_CUDA(cudaMemcpyAsync(&dev_err, out + 3, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NOALLOC_CUDA(cudaStreamSynchronize(stream));
+    if (dev_err != 0) return noalloc_fail(MDSX_ETIMEOUT, "a bounded device wait in the sweep kernel timed out");
+    return MDSX_OK;
+}
+
+}  // extern "C"

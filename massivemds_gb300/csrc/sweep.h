@@ -6,6 +6,8 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "sweep_kernel.cuh"
 
 namespace mdsx {
@@ -44,6 +46,9 @@ MDSX_DECLARE_MODE(f32)
 MDSX_DECLARE_MODE(f64)
 MDSX_DECLARE_MODE(f64s32)
 #undef MDSX_DECLARE_MODE
+
+// Sets the message mdsx_last_error(NULL) returns on this thread (engine.cu).
+void set_global_error(const std::string& msg);
 
 // Preprocessing kernels (prep.cu).
 // Row-major double locations [n][p] -> SoA [p][x_ld] in the compute type; columns >= n zeroed.
