@@ -135,6 +135,50 @@ int mdsx_evaluate_device(mdsx_engine* engine, double* d_sum, double* d_gradient)
 /* Number of kernel launches the last sweep issued (for launch accounting). */
 int mdsx_last_launch_count(mdsx_engine* engine, int* out);
 
+/* ---- Hamiltonian Monte Carlo (no counterpart in the reference's C++ engine;
+ * restates the R sampler hmcsampler, R/Untitled.R:477-729) ----
+ * Runs a whole chain on the engine's GPU: momentum N(0, I), leapfrog with one
+ * fused sweep per step, Metropolis accept on the FP64 Hamiltonian difference,
+ * optional Metropolis step on the precision tau (|U(tau - h, tau + h)|
+ * proposal) and Gibbs draw of the P x P trait precision
+ * (Wishart(P + N, (I + X'X)^-1)); prior on locations: matrix normal with row
+ * covariance I_N and column precision Lambda (initially I_P). The engine must
+ * hold delta and tau. Trace: `iterations` rows of MDSX_HMC_TRACE_BASE columns
+ * (log-likelihood, log prior, potential, tau, accepted, step size, Hamiltonian
+ * difference) followed by the traced pair distances and location norms. */
+#define MDSX_HMC_TRACE_BASE 7
+typedef struct {
+    int iterations;
+    int burn_in;              /* step size adapts over these if adapt_step_size */
+    int leapfrog_steps;       /* the reference uses 20 */
+    double step_size;         /* initial; the reference uses trajectory / 20 = 0.01 */
+    int adapt_step_size;      /* dual averaging during burn-in */
+    double target_accept;     /* e.g. 0.8 */
+    int learn_precision;      /* Metropolis step on tau each iteration */
+    double precision_half_width; /* the reference uses 0.01 */
+    int learn_trait_precision;   /* Gibbs draw of the trait precision each iteration */
+    unsigned long long seed;
+    int n_traced_pairs;          /* distances |x_i - x_j| traced per iteration */
+    const int* traced_pairs;     /* 2 * n_traced_pairs location indices */
+    int n_traced_locations;      /* norms |x_i| traced per iteration */
+    const int* traced_locations;
+    int use_graph;               /* capture each trajectory as a CUDA graph */
+} mdsx_hmc_config;
+
+typedef struct {
+    double accept_rate;              /* after burn-in */
+    double step_size;                /* final */
+    double seconds;                  /* wall time of the iterations after burn-in */
+    long long gradient_evaluations;  /* fused sweeps run */
+    double precision;                /* final tau */
+} mdsx_hmc_stats;
+
+/* initial_locations: N*P host doubles; trace: iterations * (MDSX_HMC_TRACE_BASE +
+ * n_traced_pairs + n_traced_locations) host doubles; final_locations (N*P) and
+ * stats may be NULL. The engine is left at the final locations and precision. */
+int mdsx_hmc_run(mdsx_engine* engine, const mdsx_hmc_config* config, const double* initial_locations,
+                 double* trace, double* final_locations, mdsx_hmc_stats* stats);
+
 /* ---- Allocation-free variant (no counterpart in the reference) ----
  * For callers that cannot allocate device memory: hosts whose GPU memory is
  * owned by another allocator (a JVM or R process sharing the device with a

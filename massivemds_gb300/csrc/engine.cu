@@ -27,58 +27,13 @@
 
 #include "../../include/mdsx.h"
 #include "normal_rational.h"
+#include "engine_internal.h"
 #include "sweep.h"
 
-using mdsx::KernelShape;
-using mdsx::Mode;
-using mdsx::SweepArgs;
 
-struct mdsx_engine {
-    int p = 0, n = 0;
-    long flags = 0;
-    int device = 0;
-    bool trunc = false;
-    Mode mode = Mode::kF64;
-    bool delta_f32 = false, x_f32 = false;
 
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    int sm_count = 0;
-
-    KernelShape shape{};
-    int n_row_blocks = 0, rows_padded = 0, steps_per_row = 0, grid = 0, max_slots = 0;
-    long long n_units = 0;
-
-    void* d_delta = nullptr;
-    long long ld = 0;
-    void* d_x[2] = {nullptr, nullptr};
-    int x_ld = 0;
-    int xcur = 0;
-    double* d_xin = nullptr;
-    double* d_grad[2] = {nullptr, nullptr};
-    int gcur = 0;
-    double* d_out = nullptr;  // [0] r2, [1] logPhi, [2] sumOfIncrements, [3] error word (int)
-    void* d_gpart = nullptr;
-    double* d_lpart = nullptr;
-    double* d_lrow = nullptr;
-    unsigned* d_counts = nullptr;  // [n_row_blocks] + [1]
-    int* d_row_nan = nullptr;
-    double* h_out = nullptr;  // pinned mirror of d_out
-
-    CUtensorMap tmap_delta{};
-    CUtensorMap tmap_x[2]{};
-
-    bool data_set = false;
-    double tau = 0.0, stored_tau = 0.0;
-    bool sum_known = false;
-    double sum_r2 = 0.0, sum_log = 0.0;  // last computed (ordered-pair, unscaled) sums
-    double stored_sum_r2 = 0.0, stored_sum_log = 0.0;
-    bool grad_known = false, stored_grad_known = false;
-    int last_launches = 0;
-    std::string last_error;
-};
-
-namespace {
+namespace mdsx {
+namespace internal {
 
 thread_local std::string g_create_error;
 
@@ -94,25 +49,6 @@ int cuda_fail(mdsx_engine* e, cudaError_t err, const char* what) {
     std::string msg = std::string(what) + ": " + cudaGetErrorString(err);
     return fail(e, err == cudaErrorMemoryAllocation ? MDSX_ENOMEM : MDSX_ECUDA, msg);
 }
-
-#define MDSX_CUDA(e, call)                                \
-    do {                                                  \
-        cudaError_t _err = (call);                        \
-        if (_err != cudaSuccess) return cuda_fail(e, _err, #call); \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    bool changed = false;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
-            changed = cudaSetDevice(dev) == cudaSuccess;
-        }
-    }
-    ~DeviceGuard() {
-        if (changed) cudaSetDevice(prev);
-    }
-};
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -307,7 +243,10 @@ double sum_of_increments(const mdsx_engine* e) {
     return 0.5 * e->tau * half_r2;
 }
 
-}  // namespace
+}  // namespace internal
+}  // namespace mdsx
+
+using namespace mdsx::internal;
 
 extern "C" {
 

@@ -1,0 +1,93 @@
+// Engine state shared by the translation units of libmdsx.so (engine.cu, hmc.cu).
+// Not part of the public ABI.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/mdsx.h"
+#include "sweep.h"
+
+using mdsx::KernelShape;
+using mdsx::Mode;
+using mdsx::SweepArgs;
+
+struct mdsx_engine {
+    int p = 0, n = 0;
+    long flags = 0;
+    int device = 0;
+    bool trunc = false;
+    Mode mode = Mode::kF64;
+    bool delta_f32 = false, x_f32 = false;
+
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+
+    KernelShape shape{};
+    int n_row_blocks = 0, rows_padded = 0, steps_per_row = 0, grid = 0, max_slots = 0;
+    long long n_units = 0;
+
+    void* d_delta = nullptr;
+    long long ld = 0;
+    void* d_x[2] = {nullptr, nullptr};
+    int x_ld = 0;
+    int xcur = 0;
+    double* d_xin = nullptr;
+    double* d_grad[2] = {nullptr, nullptr};
+    int gcur = 0;
+    double* d_out = nullptr;  // [0] r2, [1] logPhi, [2] sumOfIncrements, [3] error word (int)
+    void* d_gpart = nullptr;
+    double* d_lpart = nullptr;
+    double* d_lrow = nullptr;
+    unsigned* d_counts = nullptr;  // [n_row_blocks] + [1]
+    int* d_row_nan = nullptr;
+    double* h_out = nullptr;  // pinned mirror of d_out
+
+    CUtensorMap tmap_delta{};
+    CUtensorMap tmap_x[2]{};
+
+    bool data_set = false;
+    double tau = 0.0, stored_tau = 0.0;
+    bool sum_known = false;
+    double sum_r2 = 0.0, sum_log = 0.0;  // last computed (ordered-pair, unscaled) sums
+    double stored_sum_r2 = 0.0, stored_sum_log = 0.0;
+    bool grad_known = false, stored_grad_known = false;
+    int last_launches = 0;
+    std::string last_error;
+};
+
+namespace mdsx {
+namespace internal {
+
+int fail(mdsx_engine* e, int code, const std::string& msg);
+int cuda_fail(mdsx_engine* e, cudaError_t err, const char* what);
+
+#define MDSX_CUDA(e, call)                                              \
+    do {                                                                \
+        cudaError_t _err = (call);                                      \
+        if (_err != cudaSuccess) return mdsx::internal::cuda_fail(e, _err, #call); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) changed = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+// Enqueues one fused sweep at the current state (no synchronisation).
+int enqueue_sweep(mdsx_engine* e);
+// Runs a sweep and reads its sums back; sum and gradient become known.
+int sweep_and_read(mdsx_engine* e);
+// getSumOfIncrements() from the cached sums and the current precision.
+double sum_of_increments(const mdsx_engine* e);
+
+}  // namespace internal
+}  // namespace mdsx

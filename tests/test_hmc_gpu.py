@@ -1,0 +1,111 @@
+"""GPU tests of the on-device HMC driver (mdsx_hmc_run) against the numpy
+restatement of one trajectory (oracle/hmc_oracle.py) and against the oracle's
+log-likelihood. FP64 mode: Hamiltonian difference within 1e-7 absolute and
+proposal within 1e-9 relative of the restatement."""
+import numpy as np
+import pytest
+
+import oracle
+from massivemds_gb300 import Engine, flags as F
+from massivemds_gb300.hmc import hmc
+from oracle import hmc_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(n, p, seed, clusters=0):
+    rng = np.random.default_rng(seed)
+    y = rng.standard_normal((n, 6)) + (3.0 * rng.standard_normal((clusters, 6))[np.arange(n) % clusters] if clusters else 0)
+    delta = np.sqrt(((y[:, None] - y[None]) ** 2).sum(-1))
+    x0 = 0.5 * rng.standard_normal((n, p))
+    return delta, x0
+
+
+def _engine(delta, p, tau, flags):
+    e = Engine(p, delta.shape[0], flags | F.LEFT_TRUNCATION)
+    e.setPairwiseData(delta)
+    e.setParameters([tau])
+    return e
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_one_trajectory_matches_restatement(use_graph):
+    n, p, tau, eps, steps, seed = 80, 2, 1.3, 0.004, 12, 21
+    delta, x0 = _problem(n, p, 5)
+    e = _engine(delta, p, tau, 0)
+    res = hmc(e, x0, iterations=1, leapfrog_steps=steps, step_size=eps, seed=seed, use_graph=use_graph)
+    e.close()
+    x_ref, dh_ref = hmc_oracle.trajectory(delta, x0, tau, eps, steps, seed, iteration=0)
+    assert abs(res.column("delta_h")[0] - dh_ref) < 1e-7
+    expected = x_ref if res.column("accepted")[0] == 1.0 else x0
+    assert np.abs(res.final_locations - expected).max() <= 1e-9 * max(1.0, np.abs(expected).max())
+    s = oracle.sum_of_increments(delta, res.final_locations, tau)
+    assert abs(res.column("log_likelihood")[0] - oracle.log_likelihood(s, n, tau)) < 1e-8 * abs(s)
+
+
+def test_second_iteration_uses_its_own_momentum():
+    n, p, tau, eps, steps, seed = 50, 3, 0.9, 0.003, 8, 5
+    delta, x0 = _problem(n, p, 6)
+    e = _engine(delta, p, tau, 0)
+    res = hmc(e, x0, iterations=2, leapfrog_steps=steps, step_size=eps, seed=seed)
+    e.close()
+    x1 = x0
+    for it in range(2):
+        prop, dh = hmc_oracle.trajectory(delta, x1, tau, eps, steps, seed, iteration=it)
+        assert abs(res.column("delta_h")[it] - dh) < 1e-7
+        if res.column("accepted")[it] == 1.0:
+            x1 = prop
+    assert np.abs(res.final_locations - x1).max() <= 1e-9 * max(1.0, np.abs(x1).max())
+
+
+def test_fp32_chain_consistent_with_oracle():
+    n, p, tau = 400, 2, 1.0
+    delta, x0 = _problem(n, p, 7, clusters=5)
+    e = _engine(delta.astype(np.float32), p, tau, F.FLOAT)
+    res = hmc(e, x0, iterations=30, leapfrog_steps=10, step_size=0.002, seed=3)
+    e.close()
+    s = oracle.sum_of_increments(delta.astype(np.float32), res.final_locations, tau)
+    ll = oracle.log_likelihood(s, n, tau)
+    assert abs(res.column("log_likelihood")[-1] - ll) < 1e-5 * abs(ll)
+    assert res.gradient_evaluations == 1 + 30 * 10
+
+
+def test_same_seed_same_chain():
+    n, p = 200, 2
+    delta, x0 = _problem(n, p, 8)
+    runs = []
+    for _ in range(2):
+        e = _engine(delta.astype(np.float32), p, 1.0, F.FLOAT)
+        runs.append(hmc(e, x0, iterations=20, leapfrog_steps=5, step_size=0.003, seed=11,
+                        traced_pairs=[[0, 1], [2, 3]], traced_locations=[4]))
+        e.close()
+    assert np.array_equal(runs[0].trace, runs[1].trace)
+    assert np.array_equal(runs[0].final_locations, runs[1].final_locations)
+
+
+def test_step_size_adaptation_reaches_target():
+    n, p = 500, 2
+    delta, x0 = _problem(n, p, 9, clusters=5)
+    e = _engine(delta.astype(np.float32), p, 1.0, F.FLOAT)
+    res = hmc(e, x0, iterations=400, burn_in=250, leapfrog_steps=20, step_size=0.01, adapt_step_size=True,
+              target_accept=0.8, seed=1, traced_pairs=[[0, 1]], traced_locations=[0, 7])
+    e.close()
+    assert 0.55 < res.accept_rate <= 1.0
+    assert np.all(res.column("step_size")[250:] == res.step_size)
+    assert res.pair_distances.shape == (400, 1) and res.location_norms.shape == (400, 2)
+
+
+def test_precision_and_trait_precision_moves():
+    n, p = 300, 3
+    delta, x0 = _problem(n, p, 10)
+    e = _engine(delta.astype(np.float32), p, 1.0, F.FLOAT)
+    res = hmc(e, x0, iterations=60, leapfrog_steps=10, step_size=0.002, learn_precision=True,
+              precision_half_width=0.05, learn_trait_precision=True, seed=2)
+    tau_final = res.precision
+    assert np.all(res.column("precision") > 0)
+    assert len(np.unique(res.column("precision"))) > 1
+    assert res.column("precision")[-1] == tau_final
+    # the engine is left at the chain's final state
+    s = e.getSumOfIncrements()
+    e.close()
+    assert abs(s - oracle.sum_of_increments(delta.astype(np.float32), res.final_locations, tau_final)) < 1e-5 * abs(s)
