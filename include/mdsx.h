@@ -135,6 +135,52 @@ int mdsx_evaluate_device(mdsx_engine* engine, double* d_sum, double* d_gradient)
 /* Number of kernel launches the last sweep issued (for launch accounting). */
 int mdsx_last_launch_count(mdsx_engine* engine, int* out);
 
+/* ---- Learned gradient surrogate (no counterpart in the reference) ----
+ * g_i ~= s * sum_k alpha_ik (x_i - x_{l_k}) over K landmark locations (a
+ * seeded random subset), alpha_i = MLP(features_i) with rotation-invariant
+ * features [d(x_i, x_{l_k}) - delta_{i, l_k} (scaled), delta_{i, l_k}
+ * (standardised)]. The MLP
+ * (2K -> width x layers, SiLU -> K) runs forward and backward on BF16 tensor
+ * cores with FP32 accumulation and is trained with Adam on rows (features,
+ * landmark directions, exact log-likelihood gradient) harvested from exact
+ * states. Used by mdsx_hmc_run inside trajectories only; every accept is
+ * judged with the exact potential. Requires landmarks and width multiples of
+ * 64; the surrogate reads the engine's delta and lives on its GPU and stream,
+ * and must be destroyed before the engine. */
+typedef struct mdsx_surrogate mdsx_surrogate;
+
+int mdsx_surrogate_create(mdsx_engine* engine, int landmarks, int hidden_width, int hidden_layers,
+                          int max_training_rows, unsigned long long seed, mdsx_surrogate** out);
+void mdsx_surrogate_destroy(mdsx_surrogate* surrogate);
+const char* mdsx_surrogate_last_error(const mdsx_surrogate* surrogate);
+/* ints[8]: N, P, landmarks, width, layers, harvested rows, max rows, Adam steps;
+ * reals[5]: delta-feature mean and 1/sd, contraction scale, target scale,
+ * 1/scale of the residual features. */
+int mdsx_surrogate_info(const mdsx_surrogate* surrogate, int* ints, double* reals);
+int mdsx_surrogate_landmarks(const mdsx_surrogate* surrogate, int* out);
+/* which: 0 read, 1 write the FP32 weight [out][in] and bias of `layer`
+ * (0 .. layers; `layers` is the output layer), 2 read their gradients. */
+int mdsx_surrogate_parameters(mdsx_surrogate* surrogate, int layer, int which, float* weight, float* bias);
+/* Harvest `rows` rows at random locations of one exact state (host N*P doubles). */
+int mdsx_surrogate_add_state(mdsx_surrogate* surrogate, const double* locations, const double* gradient, int rows,
+                             unsigned long long seed);
+int mdsx_surrogate_training_rows(mdsx_surrogate* surrogate, int first, int count, float* features,
+                                 float* directions, float* targets);
+/* Adam steps on seeded uniform batches (batch a multiple of 64); loss_trace
+ * (steps doubles, may be NULL) gets each step's mean squared error in units
+ * of the target scale. */
+int mdsx_surrogate_train(mdsx_surrogate* surrogate, int steps, int batch, double learning_rate,
+                         unsigned long long seed, double* loss_trace);
+/* Loss and parameter gradients of the given training rows, without update. */
+int mdsx_surrogate_batch_gradient(mdsx_surrogate* surrogate, const int* rows, int count, double* loss);
+/* Surrogate log-likelihood gradient at host locations (N*P) into host gradient. */
+int mdsx_surrogate_gradient(mdsx_surrogate* surrogate, const double* locations, double* gradient);
+/* Test hook: C[m x n] = op(A) op(B) with the MLP's tensor-core GEMM (BF16 bit
+ * patterns in, FP32 out, host buffers). a_t: A stored [k][m]; b_t: B stored
+ * [k][n] (else [n][k]); m, n multiples of 64, k of 32. */
+int mdsx_test_gemm_bf16(int a_t, int b_t, int m, int n, int k, const unsigned short* a, const unsigned short* b,
+                        float* c);
+
 /* ---- Hamiltonian Monte Carlo (no counterpart in the reference's C++ engine;
  * restates the R sampler hmcsampler, R/Untitled.R:477-729) ----
  * Runs a whole chain on the engine's GPU: momentum N(0, I), leapfrog with one
@@ -145,8 +191,8 @@ int mdsx_last_launch_count(mdsx_engine* engine, int* out);
  * covariance I_N and column precision Lambda (initially I_P). The engine must
  * hold delta and tau. Trace: `iterations` rows of MDSX_HMC_TRACE_BASE columns
  * (log-likelihood, log prior, potential, tau, accepted, step size, Hamiltonian
- * difference) followed by the traced pair distances and location norms. */
-#define MDSX_HMC_TRACE_BASE 7
+ * difference, 1 if the trajectory used the surrogate) followed by the traced pair distances and location norms. */
+#define MDSX_HMC_TRACE_BASE 8
 typedef struct {
     int iterations;
     int burn_in;              /* step size adapts over these if adapt_step_size */
@@ -163,6 +209,23 @@ typedef struct {
     int n_traced_locations;      /* norms |x_i| traced per iteration */
     const int* traced_locations;
     int use_graph;               /* capture each trajectory as a CUDA graph */
+    /* Surrogate phase (surrogate == NULL: exact gradients throughout). The
+     * first harvest_iterations iterations use exact gradients; iterations
+     * harvest_start .. harvest_iterations - 1 harvest harvest_rows rows from
+     * the chain's state after the accept step (finite by construction); the
+     * surrogate is then trained (train_steps Adam steps, train_batch rows,
+     * train_learning_rate) and drives the leapfrog steps. When the acceptance
+     * rate over the last fallback_window surrogate iterations drops below
+     * fallback_accept the chain returns to exact gradients for good. */
+    mdsx_surrogate* surrogate;
+    int harvest_iterations;
+    int harvest_start;
+    int harvest_rows;
+    int train_steps;
+    int train_batch;
+    double train_learning_rate;
+    double fallback_accept;      /* 0.6 */
+    int fallback_window;         /* e.g. 50 */
 } mdsx_hmc_config;
 
 typedef struct {
@@ -171,6 +234,10 @@ typedef struct {
     double seconds;                  /* wall time of the iterations after burn-in */
     long long gradient_evaluations;  /* fused sweeps run */
     double precision;                /* final tau */
+    long long surrogate_evaluations; /* surrogate gradients evaluated */
+    int fallback_iteration;          /* iteration of the fallback to exact gradients, -1 if none */
+    double train_seconds;            /* wall time of surrogate training */
+    double train_loss;               /* mean loss over the last 10% of training steps */
 } mdsx_hmc_stats;
 
 /* initial_locations: N*P host doubles; trace: iterations * (MDSX_HMC_TRACE_BASE +

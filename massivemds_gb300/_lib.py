@@ -50,6 +50,19 @@ SIGNATURES = {
     "mdsx_hmc_run": (_i, [_vp, _vp, _dp, _dp, _dp, _vp]),
     "mdsx_sweep_f32_noalloc": (_i, [_vp, ctypes.c_longlong, _vp, _i, _i, ctypes.c_double, _i, _vp, _vp, _vp]),
     "mdsx_version": (ctypes.c_char_p, []),
+    "mdsx_surrogate_create": (_i, [_vp, _i, _i, _i, _i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
+    "mdsx_surrogate_destroy": (None, [_vp]),
+    "mdsx_surrogate_last_error": (ctypes.c_char_p, [_vp]),
+    "mdsx_surrogate_info": (_i, [_vp, _ip, _dp]),
+    "mdsx_surrogate_landmarks": (_i, [_vp, _ip]),
+    "mdsx_surrogate_parameters": (_i, [_vp, _i, _i, _fp, _fp]),
+    "mdsx_surrogate_add_state": (_i, [_vp, _dp, _dp, _i, ctypes.c_ulonglong]),
+    "mdsx_surrogate_training_rows": (_i, [_vp, _i, _i, _fp, _fp, _fp]),
+    "mdsx_surrogate_train": (_i, [_vp, _i, _i, ctypes.c_double, ctypes.c_ulonglong, _dp]),
+    "mdsx_surrogate_batch_gradient": (_i, [_vp, _ip, _i, _dp]),
+    "mdsx_surrogate_gradient": (_i, [_vp, _dp, _dp]),
+    "mdsx_test_gemm_bf16": (_i, [_i, _i, _i, _i, _i, ctypes.POINTER(ctypes.c_ushort),
+                                 ctypes.POINTER(ctypes.c_ushort), _fp]),
 }
 
 _lib = None

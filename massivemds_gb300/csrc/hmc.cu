@@ -21,7 +21,13 @@
 //   - after an accepted tau move or a Lambda draw the current potential is
 //     recomputed; the reference keeps the stale value (:676-686, :694-700);
 //   - the step size may be tuned during burn-in by dual averaging (Hoffman and
-//     Gelman 2014, Algorithm 5) toward a target acceptance rate.
+//     Gelman 2014, Algorithm 5) toward a target acceptance rate;
+//   - optionally (no reference counterpart) a learned gradient surrogate
+//     (surrogate.cu) drives the leapfrog steps after a harvest phase. Any
+//     deterministic vector field in the kicks keeps leapfrog volume-preserving
+//     and reversible, and the accept uses the exact potential at the proposal,
+//     so the chain still targets the exact posterior. The first half-kick
+//     uses the surrogate at the start point too, for reversibility.
 //
 // Everything per location stays on the GPU. Each leapfrog step is one fused
 // sweep (likelihood + gradient) and one kick/drift kernel that also writes the
@@ -41,6 +47,7 @@
 
 #include "../../include/mdsx.h"
 #include "engine_internal.h"
+#include "surrogate.h"
 
 namespace mdsx {
 namespace hmc {
@@ -389,9 +396,12 @@ struct Chain {
     double *partial = nullptr, *red_k0 = nullptr, *red_k = nullptr, *red_q = nullptr, *func = nullptr;
     int *pairs = nullptr, *locs = nullptr;
     double* h = nullptr;  // pinned: [0..3] sums, [4] K0, [5] K*, [6..] X'X* and Q*, then functionals
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    bool graph_dirty = true;
+    double *gs0 = nullptr, *gsur = nullptr;  // surrogate gradients at x0 and at the proposal
+    double* xq = nullptr;                    // second position buffer of surrogate trajectories
+    double* xfinal = nullptr;                // the buffer holding the last trajectory's proposal
+    cudaGraph_t graph = nullptr, graph_s = nullptr;
+    cudaGraphExec_t exec = nullptr, exec_s = nullptr;
+    bool graph_dirty = true, graph_s_dirty = true;
     Lambda lam{};
     double logdet_lam = 0.0;
     double eps = 0.0;
@@ -407,6 +417,11 @@ struct Chain {
     ~Chain() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        if (exec_s) cudaGraphExecDestroy(exec_s);
+        if (graph_s) cudaGraphDestroy(graph_s);
+        cudaFree(gs0);
+        cudaFree(gsur);
+        cudaFree(xq);
         cudaFree(x0);
         cudaFree(xp);
         cudaFree(mom);
@@ -429,6 +444,11 @@ struct Chain {
         MDSX_CUDA(e, cudaMalloc(&mom, xb));
         MDSX_CUDA(e, cudaMalloc(&gl0, xb));
         MDSX_CUDA(e, cudaMalloc(&coef, 6 * sizeof(double)));
+        if (cfg.surrogate) {
+            MDSX_CUDA(e, cudaMalloc(&gs0, xb));
+            MDSX_CUDA(e, cudaMalloc(&gsur, xb));
+            MDSX_CUDA(e, cudaMalloc(&xq, xb));
+        }
         MDSX_CUDA(e, cudaMalloc(&partial, (size_t)kReduceBlocks * kMaxReduce * sizeof(double)));
         MDSX_CUDA(e, cudaMalloc(&red_k0, kMaxReduce * sizeof(double)));
         MDSX_CUDA(e, cudaMalloc(&red_k, kMaxReduce * sizeof(double)));
@@ -473,17 +493,34 @@ struct Chain {
     }
 
     // The trajectory from x0 (momentum already drawn): xp, mom end at the
-    // proposal; sums, K* and X'X*, Q* land in the pinned host buffer.
-    int enqueue_trajectory() {
+    // proposal; sums, K* and X'X*, Q* land in the pinned host buffer. With
+    // `surr` the kicks use the surrogate gradient (gs0 at x0, gsur after each
+    // drift) and one exact sweep at the proposal gives its potential.
+    int enqueue_trajectory(bool surr) {
         const int L = cfg.leapfrog_steps;
         MDSX_CUDA(e, cudaMemcpyAsync(xp, x0, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        int rc = kick_drift(xp, gl0, coef);
-        for (int k = 1; !rc && k <= L; ++k) {
-            rc = internal::enqueue_sweep(e);
-            if (!rc) rc = kick_drift(xp, e->d_grad[e->gcur], k < L ? coef + 2 : coef + 4);
+        int rc = kick_drift(xp, surr ? gs0 : gl0, coef);
+        xfinal = xp;
+        if (surr) {
+            // fused surrogate steps: positions ping-pong between xp and xq
+            double* cur = xp;
+            double* nxt = xq;
+            for (int k = 1; !rc && k <= L; ++k) {
+                rc = surr::kick_drift(cfg.surrogate, cur, nxt, mom, k == L ? gsur : nullptr, k < L ? coef + 2 : coef + 4,
+                                      lam.m, s);
+                if (rc) e->last_error = cfg.surrogate->last_error;
+                std::swap(cur, nxt);
+            }
+            xfinal = cur;
+            if (!rc) rc = internal::enqueue_sweep(e);  // exact potential at the proposal
+        } else {
+            for (int k = 1; !rc && k <= L; ++k) {
+                rc = internal::enqueue_sweep(e);
+                if (!rc) rc = kick_drift(xp, e->d_grad[e->gcur], k < L ? coef + 2 : coef + 4);
+            }
         }
         if (!rc) rc = reduce(0, mom, red_k);
-        if (!rc) rc = reduce(1, xp, red_q);
+        if (!rc) rc = reduce(1, xfinal, red_q);
         if (rc) return rc;
         MDSX_CUDA(e, cudaMemcpyAsync(h_sums(), e->d_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
         MDSX_CUDA(e, cudaMemcpyAsync(h_k(), red_k, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -491,15 +528,19 @@ struct Chain {
         return MDSX_OK;
     }
 
-    int run_trajectory() {
-        if (!cfg.use_graph) return enqueue_trajectory();
-        if (graph_dirty) {
-            if (exec) cudaGraphExecDestroy(exec);
-            if (graph) cudaGraphDestroy(graph);
-            exec = nullptr;
-            graph = nullptr;
+    int run_trajectory(bool surr) {
+        if (!cfg.use_graph) return enqueue_trajectory(surr);
+        xfinal = (surr && cfg.leapfrog_steps % 2 == 1) ? xq : xp;  // as enqueue_trajectory leaves it
+        cudaGraph_t& gr = surr ? graph_s : graph;
+        cudaGraphExec_t& ex = surr ? exec_s : exec;
+        bool& dirty = surr ? graph_s_dirty : graph_dirty;
+        if (dirty) {
+            if (ex) cudaGraphExecDestroy(ex);
+            if (gr) cudaGraphDestroy(gr);
+            ex = nullptr;
+            gr = nullptr;
             MDSX_CUDA(e, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            const int rc = enqueue_trajectory();
+            const int rc = enqueue_trajectory(surr);
             cudaGraph_t g = nullptr;
             const cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (rc) {
@@ -507,11 +548,11 @@ struct Chain {
                 return rc;
             }
             MDSX_CUDA(e, ce);
-            graph = g;
-            MDSX_CUDA(e, cudaGraphInstantiate(&exec, graph, 0));
-            graph_dirty = false;
+            gr = g;
+            MDSX_CUDA(e, cudaGraphInstantiate(&ex, gr, 0));
+            dirty = false;
         }
-        MDSX_CUDA(e, cudaGraphLaunch(exec, s));
+        MDSX_CUDA(e, cudaGraphLaunch(ex, s));
         return MDSX_OK;
     }
 
@@ -541,6 +582,7 @@ struct Chain {
         logdet_lam = log_det_spd(m, p);
         if (!std::isfinite(logdet_lam)) return fail(e, MDSX_EINVAL, "trait precision is not positive definite");
         graph_dirty = true;
+        graph_s_dirty = true;
         return MDSX_OK;
     }
 };
@@ -573,6 +615,15 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         return fail(e, MDSX_EINVAL, "hmc: precision_half_width must be > 0");
     if (cfg->adapt_step_size && !(cfg->target_accept > 0.0 && cfg->target_accept < 1.0))
         return fail(e, MDSX_EINVAL, "hmc: target_accept must be in (0, 1)");
+    if (cfg->surrogate) {
+        if (cfg->surrogate->engine != e) return fail(e, MDSX_EINVAL, "hmc: the surrogate belongs to another engine");
+        if (cfg->harvest_iterations < 0 || cfg->harvest_iterations > cfg->iterations || cfg->harvest_rows < 0 ||
+            cfg->harvest_start < 0 ||
+            cfg->train_steps < 0 || cfg->fallback_window < 1 || !(cfg->fallback_accept >= 0.0 && cfg->fallback_accept <= 1.0))
+            return fail(e, MDSX_EINVAL, "hmc: bad surrogate configuration");
+        if (cfg->train_steps > 0 && !(cfg->train_learning_rate > 0.0))
+            return fail(e, MDSX_EINVAL, "hmc: train_learning_rate must be > 0");
+    }
 
     mdsx::internal::DeviceGuard guard(e->device);
     Chain c;
@@ -617,6 +668,38 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
     long long accepted_after = 0;
     auto t_start = std::chrono::steady_clock::now();
     bool timing = cfg->burn_in == 0;
+    // surrogate phase
+    mdsx_surrogate* const sg = cfg->surrogate;
+    bool surr_ready = false;
+    int fallback_it = -1;
+    long long surr_evals = 0;
+    double train_seconds = 0.0, train_loss = NAN;
+    std::vector<char> window;  // accept flags of recent surrogate iterations (ring)
+    int window_pos = 0, window_sum = 0;
+    auto start_surrogate = [&]() -> int {
+        const auto t0 = std::chrono::steady_clock::now();
+        std::vector<double> losses(std::max(1, cfg->train_steps));
+        int r = MDSX_OK;
+        if (cfg->train_steps > 0)
+            r = mdsx_surrogate_train(sg, cfg->train_steps, cfg->train_batch, cfg->train_learning_rate, cfg->seed + 17,
+                                     losses.data());
+        if (!r) r = mdsx::surr::gradient(sg, c.x0, c.gs0, c.s);
+        if (r) {
+            e->last_error = sg->last_error;
+            return r;
+        }
+        MDSX_CUDA(e, cudaStreamSynchronize(c.s));
+        train_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (cfg->train_steps > 0) {
+            const int tail = std::max(1, cfg->train_steps / 10);
+            double acc = 0.0;
+            for (int k = cfg->train_steps - tail; k < cfg->train_steps; ++k) acc += losses[k];
+            train_loss = acc / tail;
+        }
+        surr_ready = true;
+        return MDSX_OK;
+    };
+    if (sg && cfg->harvest_iterations == 0 && (rc = start_surrogate())) return rc;
 
     for (int it = 0; it < cfg->iterations; ++it) {
         if (!timing && it == cfg->burn_in) {
@@ -632,11 +715,16 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
             if ((rc = c.reduce(0, c.mom, c.red_k0))) return rc;
             MDSX_CUDA(e, cudaMemcpyAsync(c.h_k0(), c.red_k0, sizeof(double), cudaMemcpyDeviceToHost, c.s));
         }
-        if ((rc = c.run_trajectory())) return rc;
+        const bool use_surr = surr_ready && fallback_it < 0;
+        if ((rc = c.run_trajectory(use_surr))) return rc;
         MDSX_CUDA(e, cudaStreamSynchronize(c.s));
         if ((rc = c.check_device_error())) return rc;
-        c.sweeps += cfg->leapfrog_steps;
-
+        if (use_surr) {
+            c.sweeps += 1;
+            surr_evals += cfg->leapfrog_steps;
+        } else {
+            c.sweeps += cfg->leapfrog_steps;
+        }
         const double loglik_p = c.log_likelihood(c.h_sums()[2]);
         const double logprior_p = c.log_prior(c.h_q()[p * p]);
         const double u_p = -(loglik_p + logprior_p);
@@ -645,15 +733,40 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         const double alpha = std::isfinite(dh) ? std::min(1.0, std::exp(dh)) : 0.0;
         const double eps_used = c.eps;
         if (accept) {
-            MDSX_CUDA(e, cudaMemcpyAsync(c.x0, c.xp, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
+            MDSX_CUDA(e, cudaMemcpyAsync(c.x0, c.xfinal, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
             MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, e->d_grad[e->gcur], (size_t)n * p * sizeof(double),
                                          cudaMemcpyDeviceToDevice, c.s));
+            if (use_surr)
+                MDSX_CUDA(e, cudaMemcpyAsync(c.gs0, c.gsur, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToDevice,
+                                             c.s));
             loglik0 = loglik_p;
             logprior0 = logprior_p;
             u0 = u_p;
             s0.assign(c.h_q(), c.h_q() + p * p);
         }
         if (it >= cfg->burn_in && accept) ++accepted_after;
+        // harvest (chain state, its exact gradient)
+        if (sg && it >= cfg->harvest_start && it < cfg->harvest_iterations && cfg->harvest_rows > 0) {
+            rc = mdsx::surr::add_state(sg, c.x0, c.gl0, cfg->harvest_rows,
+                                       cfg->seed * 0x9E3779B97F4A7C15ULL + (unsigned long long)it, c.s);
+            if (rc) {
+                e->last_error = sg->last_error;
+                return rc;
+            }
+        }
+        if (use_surr) {  // rolling acceptance and fallback to exact gradients
+            if ((int)window.size() < cfg->fallback_window) {
+                window.push_back(accept);
+                window_sum += accept;
+            } else {
+                window_sum += (int)accept - window[window_pos];
+                window[window_pos] = accept;
+                window_pos = (window_pos + 1) % cfg->fallback_window;
+            }
+            if ((int)window.size() == cfg->fallback_window &&
+                window_sum < cfg->fallback_accept * cfg->fallback_window)
+                fallback_it = it;
+        }
 
         if (cfg->adapt_step_size && it < cfg->burn_in) {
             const double m = it + 1;
@@ -684,6 +797,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
                 MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, e->d_grad[e->gcur], (size_t)n * p * sizeof(double),
                                              cudaMemcpyDeviceToDevice, c.s));
                 c.graph_dirty = true;  // the captured sweeps hold the old precision
+                c.graph_s_dirty = true;
             } else {
                 e->tau = tau_old;
             }
@@ -703,6 +817,9 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
             u0 = -(loglik0 + logprior0);
         }
 
+        // end of the harvest phase: train, then start from the surrogate gradient at x0
+        if (sg && !surr_ready && it + 1 == cfg->harvest_iterations && (rc = start_surrogate())) return rc;
+
         // trace row
         double* row = trace + (size_t)it * cols;
         row[0] = loglik0;
@@ -712,6 +829,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         row[4] = accept ? 1.0 : 0.0;
         row[5] = eps_used;
         row[6] = dh;
+        row[7] = use_surr ? 1.0 : 0.0;
         if (c.n_func) {
             MDSX_CUDA(e, with_p(p, FunctionalsF{c.x0, c.pairs, cfg->n_traced_pairs, c.locs, cfg->n_traced_locations,
                                                  c.func, c.s}));
@@ -738,6 +856,10 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         stats->seconds = seconds;
         stats->gradient_evaluations = c.sweeps;
         stats->precision = e->tau;
+        stats->surrogate_evaluations = surr_evals;
+        stats->fallback_iteration = fallback_it;
+        stats->train_seconds = train_seconds;
+        stats->train_loss = train_loss;
     }
     return MDSX_OK;
 }

@@ -96,3 +96,23 @@ def clustered_delta(n: int, dim: int = 10, clusters: int = 5, noise_sd: float = 
 
 def locations(n: int, p: int, seed: int) -> np.ndarray:
     return np.random.default_rng(seed).standard_normal((n, p))
+
+
+def classical_mds(delta: np.ndarray, p: int, iterations: int = 60, seed: int = 0) -> np.ndarray:
+    """Classical (Torgerson) MDS start: the top-p eigenvectors of
+    B = -1/2 J delta^2 J by subspace iteration, scaled by the square roots of
+    their eigenvalues. Used only to start chains near the posterior mode."""
+    n = delta.shape[0]
+    d2 = np.square(delta, dtype=np.float32)
+
+    def bmul(v):
+        v = v - v.mean(0)
+        w = d2 @ v.astype(np.float32)
+        w = w.astype(np.float64)
+        return -0.5 * (w - w.mean(0))
+
+    v = np.linalg.qr(np.random.default_rng(seed).standard_normal((n, p)))[0]
+    for _ in range(iterations):
+        v = np.linalg.qr(bmul(v))[0]
+    lam = np.maximum(np.einsum("ip,ip->p", v, bmul(v)), 0.0)
+    return v * np.sqrt(lam)

@@ -16,8 +16,9 @@ import numpy as np
 from ._lib import check, load
 from .engine import Engine
 
-TRACE_BASE = 7
-TRACE_COLUMNS = ("log_likelihood", "log_prior", "potential", "precision", "accepted", "step_size", "delta_h")
+TRACE_BASE = 8
+TRACE_COLUMNS = ("log_likelihood", "log_prior", "potential", "precision", "accepted", "step_size", "delta_h",
+                 "surrogate")
 
 
 class _Config(ctypes.Structure):
@@ -37,6 +38,15 @@ class _Config(ctypes.Structure):
         ("n_traced_locations", ctypes.c_int),
         ("traced_locations", ctypes.POINTER(ctypes.c_int)),
         ("use_graph", ctypes.c_int),
+        ("surrogate", ctypes.c_void_p),
+        ("harvest_iterations", ctypes.c_int),
+        ("harvest_start", ctypes.c_int),
+        ("harvest_rows", ctypes.c_int),
+        ("train_steps", ctypes.c_int),
+        ("train_batch", ctypes.c_int),
+        ("train_learning_rate", ctypes.c_double),
+        ("fallback_accept", ctypes.c_double),
+        ("fallback_window", ctypes.c_int),
     ]
 
 
@@ -47,6 +57,10 @@ class _Stats(ctypes.Structure):
         ("seconds", ctypes.c_double),
         ("gradient_evaluations", ctypes.c_longlong),
         ("precision", ctypes.c_double),
+        ("surrogate_evaluations", ctypes.c_longlong),
+        ("fallback_iteration", ctypes.c_int),
+        ("train_seconds", ctypes.c_double),
+        ("train_loss", ctypes.c_double),
     ]
 
 
@@ -61,6 +75,10 @@ class HmcResult:
     precision: float
     n_pairs: int
     n_locations: int
+    surrogate_evaluations: int = 0
+    fallback_iteration: int = -1
+    train_seconds: float = 0.0
+    train_loss: float = float("nan")
 
     def column(self, name: str) -> np.ndarray:
         return self.trace[:, TRACE_COLUMNS.index(name)]
@@ -77,11 +95,21 @@ class HmcResult:
 def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, leapfrog_steps: int = 20,
         step_size: float = 0.01, adapt_step_size: bool = False, target_accept: float = 0.8,
         learn_precision: bool = False, precision_half_width: float = 0.01, learn_trait_precision: bool = False,
-        seed: int = 666, traced_pairs=None, traced_locations=None, use_graph: bool = True) -> HmcResult:
+        seed: int = 666, traced_pairs=None, traced_locations=None, use_graph: bool = True, surrogate=None,
+        harvest_iterations: int = 0, harvest_start: int | None = None, harvest_rows: int = 100, train_steps: int = 2000, train_batch: int = 512,
+        train_learning_rate: float = 1e-3, fallback_accept: float = 0.6, fallback_window: int = 50) -> HmcResult:
     """Runs one chain on the engine's GPU; the engine must hold delta and tau.
 
     Defaults follow the reference: 20 leapfrog steps of 0.01 (trajectory 0.2,
     R/Untitled.R:509-510), precision proposal half-width 0.01 (:670).
+
+    With a ``Surrogate``: the first ``harvest_iterations`` iterations use exact
+    gradients, and those from ``harvest_start`` (default: half-way) harvest
+    ``harvest_rows`` rows from the chain's state after each accept step; the
+    surrogate is then trained (``train_*``) and drives the leapfrog kicks,
+    with the exact potential deciding every accept, until the acceptance over
+    the last ``fallback_window`` surrogate iterations drops below
+    ``fallback_accept`` (exact gradients from then on).
     """
     lib = load()
     n, p = engine.locationCount, engine.embeddingDimension
@@ -93,7 +121,10 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
     cfg = _Config(int(iterations), int(burn_in), int(leapfrog_steps), float(step_size), int(adapt_step_size),
                   float(target_accept), int(learn_precision), float(precision_half_width),
                   int(learn_trait_precision), int(seed), len(pairs), pairs.ctypes.data_as(ip), len(locs),
-                  locs.ctypes.data_as(ip), int(use_graph))
+                  locs.ctypes.data_as(ip), int(use_graph), surrogate._h.value if surrogate is not None else None,
+                  int(harvest_iterations), int(harvest_iterations // 2 if harvest_start is None else harvest_start),
+                  int(harvest_rows), int(train_steps), int(train_batch),
+                  float(train_learning_rate), float(fallback_accept), int(fallback_window))
     cols = TRACE_BASE + len(pairs) + len(locs)
     trace = np.empty((iterations, cols), dtype=np.float64)
     final = np.empty((n, p), dtype=np.float64)
@@ -103,4 +134,5 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
                            trace.ctypes.data_as(dp), final.ctypes.data_as(dp),
                            ctypes.c_void_p(ctypes.addressof(stats))), engine._h)
     return HmcResult(trace, final, stats.accept_rate, stats.step_size, stats.seconds, stats.gradient_evaluations,
-                     stats.precision, len(pairs), len(locs))
+                     stats.precision, len(pairs), len(locs), stats.surrogate_evaluations, stats.fallback_iteration,
+                     stats.train_seconds, stats.train_loss)

@@ -70,17 +70,26 @@ def grad_log_post(delta, x, tau, lam, truncation=True):
     return _o.gradient(delta, x, tau, truncation) - x @ lam
 
 
-def trajectory(delta, x0, tau, eps, steps, seed, iteration, lam=None, truncation=True):
+def trajectory(delta, x0, tau, eps, steps, seed, iteration, lam=None, truncation=True, likelihood_gradient=None):
     """One leapfrog trajectory from x0 with the GPU's momentum; returns
-    (proposal, Hamiltonian difference H(x0, p0) - H(x*, p*))."""
+    (proposal, Hamiltonian difference H(x0, p0) - H(x*, p*)).
+
+    likelihood_gradient(x), when given, replaces the exact log-likelihood
+    gradient in every kick (a surrogate); the Hamiltonian stays exact."""
     n, p = x0.shape
     lam = np.eye(p) if lam is None else lam
+
+    def grad(x):
+        if likelihood_gradient is None:
+            return grad_log_post(delta, x, tau, lam, truncation)
+        return likelihood_gradient(x) - x @ lam
+
     p0 = momentum(n * p, seed, iteration).reshape(n, p)
     x = x0.copy()
-    mom = p0 + 0.5 * eps * grad_log_post(delta, x, tau, lam, truncation)
+    mom = p0 + 0.5 * eps * grad(x)
     for k in range(1, steps + 1):
         x = x + eps * mom
-        g = grad_log_post(delta, x, tau, lam, truncation)
+        g = grad(x)
         mom = mom + (eps if k < steps else 0.5 * eps) * g
     h0 = potential(delta, x0, tau, lam, truncation) + 0.5 * np.sum(p0 * p0)
     h1 = potential(delta, x, tau, lam, truncation) + 0.5 * np.sum(mom * mom)
