@@ -246,6 +246,51 @@ typedef struct {
 int mdsx_hmc_run(mdsx_engine* engine, const mdsx_hmc_config* config, const double* initial_locations,
                  double* trace, double* final_locations, mdsx_hmc_stats* stats);
 
+/* ---- Batched multi-instance engine (replaces the reference's many-engines
+ * pattern: the JNI singleton's vector of engines addressed by index,
+ * src/jni/dr_inference_multidimensionalscaling_NativeMDSSingleton.cpp:10-100) ----
+ * Many independent MDS problems (any mix of N and P) on one GPU, evaluated by
+ * one persistent stream-K launch per embedding dimension, captured as a CUDA
+ * graph. FP32 pair arithmetic with FP64 reductions (flags must include
+ * MDSX_FLAG_FLOAT; MDSX_FLAG_LEFT_TRUNCATION applies to every instance).
+ * Instance calls keep the reference's names and lazy semantics: a getter
+ * evaluates the whole batch when any instance changed since the last
+ * evaluation. Adding an instance, setting its data or forcing a shape
+ * re-plans the batch at the next evaluation. */
+typedef struct mdsx_batch mdsx_batch;
+
+int mdsx_batch_create(long flags, int device, mdsx_batch** out);
+void mdsx_batch_destroy(mdsx_batch* batch);
+const char* mdsx_batch_last_error(const mdsx_batch* batch);
+int mdsx_batch_instance_count(const mdsx_batch* batch);
+/* JNI initialize(embeddingDimension, locationCount): *instance = new index. */
+int mdsx_batch_add_instance(mdsx_batch* batch, int embedding_dimension, int location_count, int* instance);
+int mdsx_batch_set_pairwise_data(mdsx_batch* batch, int instance, const double* data, size_t length);
+int mdsx_batch_set_pairwise_data_f32(mdsx_batch* batch, int instance, const float* data, size_t length);
+int mdsx_batch_set_parameters(mdsx_batch* batch, int instance, const double* parameters, size_t length);
+int mdsx_batch_update_locations(mdsx_batch* batch, int instance, int location_index, const double* locations,
+                                size_t length);
+int mdsx_batch_make_dirty(mdsx_batch* batch);
+int mdsx_batch_get_sum_of_increments(mdsx_batch* batch, int instance, double* out);
+int mdsx_batch_get_log_likelihood(mdsx_batch* batch, int instance, double* out);
+int mdsx_batch_get_log_likelihood_gradient(mdsx_batch* batch, int instance, double* out, size_t length);
+/* One evaluation of every instance, results read back to the host. */
+int mdsx_batch_evaluate(mdsx_batch* batch);
+/* One evaluation left on the device, enqueued without synchronising: d_sums
+ * gets [count][4] doubles (sum r^2, sum log Phi, getSumOfIncrements(),
+ * unused), d_gradients the instances' N*P gradients concatenated in instance
+ * order; either may be NULL. */
+int mdsx_batch_evaluate_device(mdsx_batch* batch, double* d_sums, double* d_gradients);
+/* Autotuner: times every built (rows per warp, CTAs per SM) shape of each
+ * dimension group on this batch and caches the fastest per (P, N-bucket =
+ * floor(log2 mean N), truncation), in process and in the file named by the
+ * environment variable MDSX_TUNE_CACHE. *candidates (may be NULL) = shapes timed. */
+int mdsx_batch_tune(mdsx_batch* batch, int repetitions, int* candidates);
+/* Shape in use for dimension p (plans the batch if needed). */
+int mdsx_batch_group_shape(mdsx_batch* batch, int p, int* rows_per_warp, int* ctas_per_sm, int* grid);
+/* Fixes the shape of dimension p's group (rows_per_warp 0 removes it). */
+int mdsx_batch_force_shape(mdsx_batch* batch, int p, int rows_per_warp, int ctas_per_sm);
+
 /* ---- Allocation-free variant (no counterpart in the reference) ----
  * For callers that cannot allocate device memory: hosts whose GPU memory is
  * owned by another allocator (a JVM or R process sharing the device with a

@@ -61,6 +61,24 @@ SIGNATURES = {
     "mdsx_surrogate_train": (_i, [_vp, _i, _i, ctypes.c_double, ctypes.c_ulonglong, _dp]),
     "mdsx_surrogate_batch_gradient": (_i, [_vp, _ip, _i, _dp]),
     "mdsx_surrogate_gradient": (_i, [_vp, _dp, _dp]),
+    "mdsx_batch_create": (_i, [_l, _i, ctypes.POINTER(_vp)]),
+    "mdsx_batch_destroy": (None, [_vp]),
+    "mdsx_batch_last_error": (ctypes.c_char_p, [_vp]),
+    "mdsx_batch_instance_count": (_i, [_vp]),
+    "mdsx_batch_add_instance": (_i, [_vp, _i, _i, _ip]),
+    "mdsx_batch_set_pairwise_data": (_i, [_vp, _i, _dp, _sz]),
+    "mdsx_batch_set_pairwise_data_f32": (_i, [_vp, _i, _fp, _sz]),
+    "mdsx_batch_set_parameters": (_i, [_vp, _i, _dp, _sz]),
+    "mdsx_batch_update_locations": (_i, [_vp, _i, _i, _dp, _sz]),
+    "mdsx_batch_make_dirty": (_i, [_vp]),
+    "mdsx_batch_get_sum_of_increments": (_i, [_vp, _i, _dp]),
+    "mdsx_batch_get_log_likelihood": (_i, [_vp, _i, _dp]),
+    "mdsx_batch_get_log_likelihood_gradient": (_i, [_vp, _i, _dp, _sz]),
+    "mdsx_batch_evaluate": (_i, [_vp]),
+    "mdsx_batch_evaluate_device": (_i, [_vp, _vp, _vp]),
+    "mdsx_batch_tune": (_i, [_vp, _i, _ip]),
+    "mdsx_batch_group_shape": (_i, [_vp, _i, _ip, _ip, _ip]),
+    "mdsx_batch_force_shape": (_i, [_vp, _i, _i, _i]),
     "mdsx_test_gemm_bf16": (_i, [_i, _i, _i, _i, _i, ctypes.POINTER(ctypes.c_ushort),
                                  ctypes.POINTER(ctypes.c_ushort), _fp]),
 }

@@ -1,0 +1,872 @@
+// Batched multi-instance engine (mdsx_batch_* of the C ABI).
+//
+// Replaces the reference's many-engines pattern, a process-wide vector of
+// independent engines addressed by index (src/jni/dr_inference_
+// multidimensionalscaling_NativeMDSSingleton.cpp:10-100: initialize,
+// updateLocations, getSumOfIncrements, getLogLikelihoodGradient,
+// setPairwiseData, setParameters, makeDirty), by one object that owns every
+// instance's data on one GPU and evaluates all of them with one persistent
+// stream-K launch per (P, truncation) group (batch_kernel.cuh), the launches
+// captured once as a CUDA graph. Results of all instances come back in one
+// device-to-host copy. Instance calls keep the reference's names and lazy
+// semantics: a getter evaluates the batch when any instance changed.
+//
+// Tile shapes (rows per warp, CTAs per SM) come from an autotuner that times
+// the candidates on the batch itself and caches the winner per (P, N-bucket,
+// truncation), in process and, when MDSX_TUNE_CACHE names a file, on disk.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/mdsx.h"
+#include "batch_sweep.h"
+#include "normal_rational.h"
+#include "sweep.h"
+
+namespace mdsx {
+namespace batch {
+
+bool rw_built(int p, int rw) {
+    if (p < 1 || p > 10) return false;
+    return rw == 1 || (rw == 2 && p <= 8) || (rw == 4 && p <= 4);
+}
+
+int smem_bytes(int p, int rw) {
+    const int rb = 8 * rw;
+    return kStages * (rb * kStepCols * 4 + p * kStepCols * 4) + 2 * kStages * 8 + 128;
+}
+
+cudaError_t occupancy(int p, bool trunc, int rw, int* ctas, size_t* local_bytes) {
+    return p <= 4 ? occupancy_lo(p, trunc, rw, ctas, local_bytes) : occupancy_hi(p, trunc, rw, ctas, local_bytes);
+}
+
+cudaError_t launch(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st) {
+    return p <= 4 ? launch_lo(p, trunc, rw, a, st) : launch_hi(p, trunc, rw, a, st);
+}
+
+namespace {
+
+// ------------------------------------------------------------ tuning cache
+
+struct TuneKey {
+    int p, bucket, trunc;
+    bool operator<(const TuneKey& o) const { return std::tie(p, bucket, trunc) < std::tie(o.p, o.bucket, o.trunc); }
+};
+struct TuneValue {
+    int rw, ctas_per_sm;
+    double us;
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneValue> g_tune;
+bool g_tune_loaded = false;
+
+// N-bucket: floor(log2(mean N)).
+int n_bucket(double mean_n) { return mean_n < 1.0 ? 0 : (int)std::floor(std::log2(mean_n)); }
+
+void load_cache_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = std::getenv("MDSX_TUNE_CACHE");
+    if (!path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    int p, b, t, rw, c;
+    double us;
+    while (std::fscanf(f, "%d %d %d %d %d %lf", &p, &b, &t, &rw, &c, &us) == 6)
+        if (rw_built(p, rw) && c >= 1 && c <= 4) g_tune[{p, b, t}] = {rw, c, us};
+    std::fclose(f);
+}
+
+void save_cache_locked() {
+    const char* path = std::getenv("MDSX_TUNE_CACHE");
+    if (!path) return;
+    FILE* f = std::fopen(path, "w");
+    if (!f) return;
+    for (const auto& kv : g_tune)
+        std::fprintf(f, "%d %d %d %d %d %.3f\n", kv.first.p, kv.first.bucket, kv.first.trunc, kv.second.rw,
+                     kv.second.ctas_per_sm, kv.second.us);
+    std::fclose(f);
+}
+
+// Default shape: the single-instance kernel's rows per warp, two CTAs per SM.
+int default_rw(int p) { return p <= 4 ? 4 : (p <= 6 ? 2 : 1); }
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+}  // namespace batch
+}  // namespace mdsx
+
+// ------------------------------------------------------------------ state
+
+struct BatchInst {
+    int p = 0, n = 0;
+    double tau = 0.0;
+    bool data_set = false;
+    float* d_delta = nullptr;  // [n][ld]
+    long long ld = 0;
+    float* d_x = nullptr;      // SoA [p][x_ld]
+    int x_ld = 0;
+    double* d_xin = nullptr;   // row-major [n][p] staging
+    // plan-dependent
+    int* d_row_nan = nullptr;
+    int rows_padded = 0, n_row_blocks = 0;
+    float* d_gpart = nullptr;
+    double* d_lpart = nullptr;
+    double* d_lrow = nullptr;
+    unsigned* d_counts = nullptr;  // [R] row-block counters + [1] done counter
+    long long grad_off = 0;        // offset (doubles) in the concatenated gradients
+};
+
+struct BatchGroup {
+    int p = 0;
+    bool trunc = false;
+    int rw = 0, ctas_per_sm = 0;
+    std::vector<int> members;
+    long long n_units = 0;
+    int grid = 0;
+    std::vector<mdsx::batch::BatchInstance> h_desc;
+    mdsx::batch::BatchInstance* d_desc = nullptr;
+    double work = 0.0;  // modelled cost: sum of N^2 x (16 + 3P) instructions per pair
+};
+
+struct mdsx_batch {
+    int device = 0;
+    long flags = 0;
+    bool trunc = false;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<BatchInst> inst;
+    std::vector<BatchGroup> groups;
+    bool planned = false, desc_dirty = true, graph_dirty = true, results_known = false;
+    double* d_grad_all = nullptr;  // concatenated gradients
+    double* d_sums_all = nullptr;  // [count][4]
+    int* d_err = nullptr;
+    double* h_results = nullptr;   // pinned: sums [count][4], then gradients
+    long long grad_total = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaStream_t> aux;     // one branch stream per dimension group (graph capture)
+    std::vector<cudaEvent_t> aux_ev;   // [0] fork, [1 + g] join of group g
+    long long evaluations = 0;
+    std::map<std::pair<int, int>, std::pair<int, int>> forced;  // (p, trunc) -> (rw, ctas per SM)
+    std::string last_error;
+};
+
+namespace {
+
+using mdsx::batch::BatchArgs;
+using mdsx::batch::BatchInstance;
+
+int bfail(mdsx_batch* b, int code, const std::string& msg) {
+    if (b) b->last_error = msg;
+    return code;
+}
+#define BCUDA(b, call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t _e = (call);                                                                        \
+        if (_e != cudaSuccess)                                                                          \
+            return bfail(b, _e == cudaErrorMemoryAllocation ? MDSX_ENOMEM : MDSX_ECUDA,                 \
+                         std::string(#call) + ": " + cudaGetErrorString(_e));                           \
+    } while (0)
+
+struct Guard {
+    int prev = -1;
+    explicit Guard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~Guard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+void free_plan_scratch(BatchInst& in) {
+    cudaFree(in.d_row_nan);
+    cudaFree(in.d_gpart);
+    cudaFree(in.d_lpart);
+    cudaFree(in.d_lrow);
+    cudaFree(in.d_counts);
+    in.d_row_nan = nullptr;
+    in.d_gpart = nullptr;
+    in.d_lpart = nullptr;
+    in.d_lrow = nullptr;
+    in.d_counts = nullptr;
+}
+
+void drop_graph(mdsx_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_dirty = true;
+}
+
+void free_plan(mdsx_batch* b) {
+    drop_graph(b);
+    for (auto& g : b->groups) cudaFree(g.d_desc);
+    b->groups.clear();
+    for (auto& in : b->inst) free_plan_scratch(in);
+    cudaFree(b->d_grad_all);
+    cudaFree(b->d_sums_all);
+    if (b->h_results) cudaFreeHost(b->h_results);
+    b->d_grad_all = nullptr;
+    b->d_sums_all = nullptr;
+    b->h_results = nullptr;
+    b->planned = false;
+}
+
+int make_tmap(mdsx_batch* b, CUtensorMap* map, void* base, long long cols, long long rows, long long ld,
+              unsigned box_cols, unsigned box_rows) {
+    auto fn = mdsx::batch::encode_tiled();
+    if (!fn) return bfail(b, MDSX_ECUDA, "cuTensorMapEncodeTiled unavailable from the driver");
+    cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)(ld * 4)};
+    cuuint32_t box[2] = {box_cols, box_rows};
+    cuuint32_t estride[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, gdim, gstride, box, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return bfail(b, MDSX_ECUDA, "cuTensorMapEncodeTiled failed");
+    return MDSX_OK;
+}
+
+// Precision constants of one instance (the single-instance engine's make_args).
+void set_precision_constants(BatchInstance& d, double tau) {
+    const double s = std::sqrt(tau);
+    d.tau = tau;
+    d.k_e = (float)(-0.5 * tau * 1.4426950408889634074);
+    d.log2_k2 = (float)std::log2(1.0 / std::sqrt(2.0 * M_PI * tau));
+    d.tp0 = (float)(mdsx::kTailP0 / tau);
+    d.tp1 = (float)(mdsx::kTailP1 / s);
+    d.tp2 = (float)mdsx::kTailP2;
+    d.ts0 = (float)(mdsx::kTailS0 / (s * s * s));
+    d.ts1 = (float)(mdsx::kTailS1 / (s * s));
+    d.ts2 = (float)(mdsx::kTailS2 / s);
+}
+
+// Builds the groups, scratch, descriptors and result buffers. `force` maps a
+// group key (p, trunc) to a shape (rw, ctas per SM) that overrides the cache.
+int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>* force = nullptr) {
+    if (b->inst.empty()) return bfail(b, MDSX_ESTATE, "batch has no instances");
+    for (size_t k = 0; k < b->inst.size(); ++k) {
+        if (!b->inst[k].data_set) return bfail(b, MDSX_ESTATE, "instance " + std::to_string(k) + ": no pairwise data");
+        if (!(b->inst[k].tau > 0.0)) return bfail(b, MDSX_ESTATE, "instance " + std::to_string(k) + ": precision not set");
+    }
+    free_plan(b);
+    cudaStream_t st = b->stream;
+    // groups by P (one truncation mode per batch)
+    std::map<int, std::vector<int>> by_p;
+    for (size_t k = 0; k < b->inst.size(); ++k) by_p[b->inst[k].p].push_back((int)k);
+    // Groups run concurrently (graph branches), each on a share of the
+    // machine proportional to its modelled cost.
+    double total_work = 0.0;
+    for (const auto& in : b->inst) total_work += (double)in.n * in.n * (16.0 + 3.0 * in.p);
+    const bool concurrent = by_p.size() > 1;
+    long long grad_off = 0;
+    for (auto& kv : by_p) {
+        BatchGroup g;
+        g.p = kv.first;
+        g.trunc = b->trunc;
+        g.members = kv.second;
+        double mean_n = 0.0;
+        for (int k : g.members) mean_n += b->inst[k].n;
+        mean_n /= g.members.size();
+        int rw = mdsx::batch::default_rw(g.p), ctas = 0;
+        {
+            std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
+            mdsx::batch::load_cache_locked();
+            auto it = mdsx::batch::g_tune.find({g.p, mdsx::batch::n_bucket(mean_n), g.trunc ? 1 : 0});
+            if (it != mdsx::batch::g_tune.end()) {
+                rw = it->second.rw;
+                ctas = it->second.ctas_per_sm;
+            }
+        }
+        if (force) {
+            auto it = force->find({g.p, g.trunc ? 1 : 0});
+            if (it != force->end()) {
+                rw = it->second.first;
+                ctas = it->second.second;
+            }
+        }
+        int occ = 0;
+        size_t local = 0;
+        BCUDA(b, mdsx::batch::occupancy(g.p, g.trunc, rw, &occ, &local));
+        if (occ < 1) return bfail(b, MDSX_ECUDA, "batched sweep kernel cannot be resident");
+        g.rw = rw;
+        g.ctas_per_sm = ctas >= 1 ? std::min(ctas, occ) : occ;
+        const int rb = 8 * rw;
+        // global units
+        for (int k : g.members) {
+            BatchInst& in = b->inst[k];
+            BatchInstance d{};
+            const int nrb = (in.n + rb - 1) / rb;
+            const int spr = (in.n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+            d.unit_begin = g.n_units;
+            d.n = in.n;
+            d.n_row_blocks = nrb;
+            d.steps_per_row = spr;
+            d.x_ld = in.x_ld;
+            d.truncation = g.trunc ? 1 : 0;
+            set_precision_constants(d, in.tau);
+            g.n_units += (long long)nrb * spr;
+            g.h_desc.push_back(d);
+        }
+        g.work = 0.0;
+        for (int k : g.members) g.work += (double)b->inst[k].n * b->inst[k].n * (16.0 + 3.0 * g.p);
+        long long slots = (long long)b->sm_count * g.ctas_per_sm;
+        if (concurrent) slots = std::max<long long>(1, std::llround(slots * g.work / total_work));
+        g.grid = (int)std::min<long long>(g.n_units, slots);
+        // per-instance slots, scratch, tensor maps
+        for (size_t m = 0; m < g.members.size(); ++m) {
+            BatchInst& in = b->inst[g.members[m]];
+            BatchInstance& d = g.h_desc[m];
+            int max_slots = 1;
+            for (int r = 0; r < d.n_row_blocks; ++r) {
+                const long long u0 = d.unit_begin + (long long)r * d.steps_per_row, u1 = u0 + d.steps_per_row - 1;
+                max_slots = std::max(max_slots, mdsx::cta_of_unit(u1, g.n_units, g.grid) -
+                                                    mdsx::cta_of_unit(u0, g.n_units, g.grid) + 1);
+            }
+            d.max_slots = max_slots;
+            in.rows_padded = d.n_row_blocks * rb;
+            in.n_row_blocks = d.n_row_blocks;
+            BCUDA(b, cudaMalloc(&in.d_row_nan, (size_t)in.rows_padded * sizeof(int)));
+            BCUDA(b, mdsx::mark_nan_rows(in.d_delta, true, in.n, in.ld, in.d_row_nan, in.rows_padded, st));
+            BCUDA(b, cudaMalloc(&in.d_gpart, (size_t)d.n_row_blocks * max_slots * rb * g.p * sizeof(float)));
+            BCUDA(b, cudaMalloc(&in.d_lpart,
+                                (size_t)d.n_row_blocks * max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
+            BCUDA(b, cudaMalloc(&in.d_lrow, (size_t)d.n_row_blocks * 2 * sizeof(double)));
+            BCUDA(b, cudaMalloc(&in.d_counts, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned)));
+            BCUDA(b, cudaMemsetAsync(in.d_counts, 0, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned), st));
+            int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
+            if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p, in.x_ld, mdsx::kStepCols, g.p);
+            if (rc) return rc;
+            d.x = in.d_x;
+            d.row_nan = in.d_row_nan;
+            d.gpart = in.d_gpart;
+            d.lpart = in.d_lpart;
+            d.lrow = in.d_lrow;
+            d.rb_count = in.d_counts;
+            d.done_count = in.d_counts + d.n_row_blocks;
+            in.grad_off = grad_off;
+            grad_off += (long long)in.n * in.p;
+        }
+        BCUDA(b, cudaMalloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
+        b->groups.push_back(std::move(g));
+    }
+    b->grad_total = grad_off;
+    const size_t count = b->inst.size();
+    BCUDA(b, cudaMalloc(&b->d_grad_all, (size_t)std::max<long long>(1, grad_off) * sizeof(double)));
+    BCUDA(b, cudaMalloc(&b->d_sums_all, count * 4 * sizeof(double)));
+    BCUDA(b, cudaMemsetAsync(b->d_sums_all, 0, count * 4 * sizeof(double), st));
+    BCUDA(b, cudaMallocHost(&b->h_results, (count * 4 + (size_t)grad_off) * sizeof(double)));
+    // output pointers (instance order in the sums array is the instance index)
+    for (auto& g : b->groups)
+        for (size_t m = 0; m < g.members.size(); ++m) {
+            const int k = g.members[m];
+            g.h_desc[m].grad_out = b->d_grad_all + b->inst[k].grad_off;
+            g.h_desc[m].sums_out = b->d_sums_all + 4 * (size_t)k;
+        }
+    while (b->aux.size() < b->groups.size()) {  // branch streams for concurrent groups (created outside capture)
+        cudaStream_t bs = nullptr;
+        BCUDA(b, cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+        b->aux.push_back(bs);
+    }
+    while (b->aux_ev.size() < b->groups.size() + 1) {
+        cudaEvent_t ev = nullptr;
+        BCUDA(b, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        b->aux_ev.push_back(ev);
+    }
+    b->planned = true;
+    b->desc_dirty = true;
+    b->graph_dirty = true;
+    BCUDA(b, cudaStreamSynchronize(st));
+    return MDSX_OK;
+}
+
+int upload_descriptors(mdsx_batch* b) {
+    for (auto& g : b->groups)
+        BCUDA(b, cudaMemcpyAsync(g.d_desc, g.h_desc.data(), g.h_desc.size() * sizeof(BatchInstance),
+                                 cudaMemcpyHostToDevice, b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));  // the host descriptors may change after return
+    b->desc_dirty = false;
+    return MDSX_OK;
+}
+
+BatchArgs group_args(const mdsx_batch* b, const BatchGroup& g) {
+    BatchArgs a{};
+    a.inst = g.d_desc;
+    a.count = (int)g.members.size();
+    a.n_units = g.n_units;
+    a.grid = g.grid;
+    a.err = b->d_err;
+    return a;
+}
+
+// The group launches: one group on the batch stream, several as concurrent
+// branches (fork from and join back to the batch stream).
+int enqueue_groups(mdsx_batch* b) {
+    if (b->groups.size() == 1) {
+        const BatchGroup& g = b->groups[0];
+        BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), b->stream));
+        return MDSX_OK;
+    }
+    if (b->aux.size() < b->groups.size() || b->aux_ev.size() < b->groups.size() + 1)
+        return bfail(b, MDSX_ESTATE, "branch streams missing (plan)");
+    BCUDA(b, cudaEventRecord(b->aux_ev[0], b->stream));
+    for (size_t i = 0; i < b->groups.size(); ++i) {
+        const BatchGroup& g = b->groups[i];
+        BCUDA(b, cudaStreamWaitEvent(b->aux[i], b->aux_ev[0], 0));
+        BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), b->aux[i]));
+        BCUDA(b, cudaEventRecord(b->aux_ev[1 + i], b->aux[i]));
+        BCUDA(b, cudaStreamWaitEvent(b->stream, b->aux_ev[1 + i], 0));
+    }
+    return MDSX_OK;
+}
+
+// Enqueues one evaluation of every instance (graph launch); no synchronisation.
+int enqueue_evaluation(mdsx_batch* b) {
+    if (!b->planned) {
+        int rc = plan(b, b->forced.empty() ? nullptr : &b->forced);
+        if (rc) return rc;
+    }
+    if (b->desc_dirty) {
+        int rc = upload_descriptors(b);
+        if (rc) return rc;
+    }
+    if (b->graph_dirty) {
+        drop_graph(b);
+        BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_groups(b);
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(b->stream, &gr);
+        if (rc) {
+            if (gr) cudaGraphDestroy(gr);
+            return rc;
+        }
+        BCUDA(b, ce);
+        b->graph = gr;
+        BCUDA(b, cudaGraphInstantiate(&b->exec, gr, 0));
+        b->graph_dirty = false;
+    }
+    BCUDA(b, cudaGraphLaunch(b->exec, b->stream));
+    ++b->evaluations;
+    return MDSX_OK;
+}
+
+// Evaluates if needed and brings every instance's sums and gradient to the host.
+int ensure_results(mdsx_batch* b) {
+    if (b->results_known) return MDSX_OK;
+    int rc = enqueue_evaluation(b);
+    if (rc) return rc;
+    const size_t count = b->inst.size();
+    BCUDA(b, cudaMemcpyAsync(b->h_results, b->d_sums_all, count * 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                             b->stream));
+    BCUDA(b, cudaMemcpyAsync(b->h_results + count * 4, b->d_grad_all, (size_t)b->grad_total * sizeof(double),
+                             cudaMemcpyDeviceToHost, b->stream));
+    int err = 0;
+    BCUDA(b, cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+    if (err) {
+        cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream);
+        for (auto& in : b->inst)
+            if (in.d_counts)
+                cudaMemsetAsync(in.d_counts, 0, ((size_t)in.n_row_blocks + 1) * sizeof(unsigned), b->stream);
+        cudaStreamSynchronize(b->stream);
+        return bfail(b, MDSX_ETIMEOUT, "a bounded device wait in the batched sweep timed out");
+    }
+    b->results_known = true;
+    return MDSX_OK;
+}
+
+int check_instance(mdsx_batch* b, int k) {
+    if (k < 0 || k >= (int)b->inst.size()) return bfail(b, MDSX_EINVAL, "instance index out of range");
+    return MDSX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdsx_batch_create(long flags, int device, mdsx_batch** out) {
+    if (!out) return MDSX_EINVAL;
+    *out = nullptr;
+    if (!(flags & MDSX_FLAG_FLOAT)) return MDSX_EUNSUPPORTED;  // the batched path computes in FP32
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return MDSX_ECUDA;
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) device = 0;
+    if (device >= count) return MDSX_EINVAL;
+    Guard guard(device);
+    auto* b = new mdsx_batch;
+    b->device = device;
+    b->flags = flags;
+    b->trunc = (flags & MDSX_FLAG_LEFT_TRUNCATION) != 0;
+    if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess || cudaMemset(b->d_err, 0, sizeof(int)) != cudaSuccess) {
+        if (b->stream) cudaStreamDestroy(b->stream);
+        cudaFree(b->d_err);
+        delete b;
+        return MDSX_ECUDA;
+    }
+    *out = b;
+    return MDSX_OK;
+}
+
+void mdsx_batch_destroy(mdsx_batch* b) {
+    if (!b) return;
+    Guard guard(b->device);
+    cudaStreamSynchronize(b->stream);
+    free_plan(b);
+    for (auto& in : b->inst) {
+        cudaFree(in.d_delta);
+        cudaFree(in.d_x);
+        cudaFree(in.d_xin);
+    }
+    cudaFree(b->d_err);
+    for (cudaStream_t st : b->aux) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->aux_ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char* mdsx_batch_last_error(const mdsx_batch* b) { return b ? b->last_error.c_str() : "NULL batch"; }
+
+int mdsx_batch_instance_count(const mdsx_batch* b) { return b ? (int)b->inst.size() : 0; }
+
+// The reference's JNI initialize(dimension, locations, ...): returns the new instance's index.
+int mdsx_batch_add_instance(mdsx_batch* b, int embedding_dimension, int location_count, int* instance) {
+    if (!b) return MDSX_EINVAL;
+    if (!instance) return bfail(b, MDSX_EINVAL, "instance is NULL");
+    if (embedding_dimension < 1 || embedding_dimension > MDSX_MAX_DIMENSION)
+        return bfail(b, MDSX_EUNSUPPORTED, "embedding dimension outside 1..MDSX_MAX_DIMENSION");
+    if (location_count < 2 || location_count > (1 << 20)) return bfail(b, MDSX_EINVAL, "locationCount outside 2..2^20");
+    Guard guard(b->device);
+    BatchInst in;
+    in.p = embedding_dimension;
+    in.n = location_count;
+    in.ld = mdsx::batch::round_up(in.n, 4);
+    in.x_ld = (int)mdsx::batch::round_up(in.n, mdsx::kStepCols);
+    const size_t xb = (size_t)in.p * in.x_ld * sizeof(float);
+    if (cudaMalloc(&in.d_delta, (size_t)in.n * in.ld * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&in.d_x, xb) != cudaSuccess ||
+        cudaMalloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
+        cudaFree(in.d_delta);
+        cudaFree(in.d_x);
+        cudaFree(in.d_xin);
+        return bfail(b, MDSX_ENOMEM, "instance allocation failed");
+    }
+    BCUDA(b, cudaMemsetAsync(in.d_x, 0, xb, b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+    *instance = (int)b->inst.size();
+    b->inst.push_back(in);
+    free_plan(b);  // the groups change
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+static int set_delta(mdsx_batch* b, int k, const float* host_rows) {
+    BatchInst& in = b->inst[k];
+    BCUDA(b, cudaMemcpy2DAsync(in.d_delta, in.ld * sizeof(float), host_rows, (size_t)in.n * sizeof(float),
+                               (size_t)in.n * sizeof(float), in.n, cudaMemcpyHostToDevice, b->stream));
+    BCUDA(b, cudaStreamSynchronize(b->stream));
+    in.data_set = true;
+    free_plan(b);  // NaN rows and tensor maps are rebuilt by the next plan
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+// setPairwiseData of one instance: N*N row-major doubles (NaN = missing), stored as FP32.
+int mdsx_batch_set_pairwise_data(mdsx_batch* b, int k, const double* data, size_t length) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    const BatchInst& in = b->inst[k];
+    if (!data || length != (size_t)in.n * in.n) return bfail(b, MDSX_EINVAL, "pairwise data must hold N*N values");
+    Guard guard(b->device);
+    std::vector<float> rows(length);
+    for (size_t i = 0; i < length; ++i) rows[i] = (float)data[i];
+    return set_delta(b, k, rows.data());
+}
+
+int mdsx_batch_set_pairwise_data_f32(mdsx_batch* b, int k, const float* data, size_t length) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    const BatchInst& in = b->inst[k];
+    if (!data || length != (size_t)in.n * in.n) return bfail(b, MDSX_EINVAL, "pairwise data must hold N*N values");
+    Guard guard(b->device);
+    return set_delta(b, k, data);
+}
+
+// setParameters of one instance: parameters[0] = precision tau > 0.
+int mdsx_batch_set_parameters(mdsx_batch* b, int k, const double* parameters, size_t length) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    if (!parameters || length < 1 || !(parameters[0] > 0.0) || !std::isfinite(parameters[0]))
+        return bfail(b, MDSX_EINVAL, "precision must be finite and > 0");
+    b->inst[k].tau = parameters[0];
+    for (auto& g : b->groups)
+        for (size_t m = 0; m < g.members.size(); ++m)
+            if (g.members[m] == k) set_precision_constants(g.h_desc[m], parameters[0]);
+    b->desc_dirty = true;
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+// updateLocations of one instance: index -1 with N*P row-major doubles, or one location (P doubles).
+int mdsx_batch_update_locations(mdsx_batch* b, int k, int index, const double* locations, size_t length) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    BatchInst& in = b->inst[k];
+    if (!locations) return bfail(b, MDSX_EINVAL, "locations is NULL");
+    Guard guard(b->device);
+    if (index == -1) {
+        if (length != (size_t)in.n * in.p) return bfail(b, MDSX_EINVAL, "locations must hold N*P values");
+        BCUDA(b, cudaMemcpyAsync(in.d_xin, locations, length * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+        BCUDA(b, mdsx::convert_locations(in.d_xin, in.n, in.p, in.d_x, in.x_ld, true, b->stream));
+    } else {
+        if (index < 0 || index >= in.n || length != (size_t)in.p)
+            return bfail(b, MDSX_EINVAL, "location index out of range or length != P");
+        BCUDA(b, cudaMemcpyAsync(in.d_xin + (size_t)index * in.p, locations, length * sizeof(double),
+                                 cudaMemcpyHostToDevice, b->stream));
+        BCUDA(b, mdsx::set_one_location(in.d_xin + (size_t)index * in.p, index, in.p, in.d_x, in.x_ld, true,
+                                        b->stream));
+    }
+    BCUDA(b, cudaStreamSynchronize(b->stream));  // the caller's buffer may change after return
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+// makeDirty: forces the next getter to evaluate again.
+int mdsx_batch_make_dirty(mdsx_batch* b) {
+    if (!b) return MDSX_EINVAL;
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+// One evaluation of every instance, results read back to the host.
+int mdsx_batch_evaluate(mdsx_batch* b) {
+    if (!b) return MDSX_EINVAL;
+    Guard guard(b->device);
+    b->results_known = false;
+    return ensure_results(b);
+}
+
+// One evaluation of every instance left on the device (no synchronisation):
+// *d_sums receives [count][4] doubles (sum r^2, sum log Phi, getSumOfIncrements(),
+// unused) and d_gradients the concatenated N_k*P_k gradients, when non-NULL.
+int mdsx_batch_evaluate_device(mdsx_batch* b, double* d_sums, double* d_gradients) {
+    if (!b) return MDSX_EINVAL;
+    Guard guard(b->device);
+    int rc = enqueue_evaluation(b);
+    if (rc) return rc;
+    if (d_sums)
+        BCUDA(b, cudaMemcpyAsync(d_sums, b->d_sums_all, b->inst.size() * 4 * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, b->stream));
+    if (d_gradients)
+        BCUDA(b, cudaMemcpyAsync(d_gradients, b->d_grad_all, (size_t)b->grad_total * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, b->stream));
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+int mdsx_batch_get_sum_of_increments(mdsx_batch* b, int k, double* out) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    if (!out) return bfail(b, MDSX_EINVAL, "out is NULL");
+    Guard guard(b->device);
+    if ((rc = ensure_results(b))) return rc;
+    *out = b->h_results[4 * (size_t)k + 2];
+    return MDSX_OK;
+}
+
+// R/mds.R:24-28: 0.5 (log tau - log 2 pi) N (N - 1) / 2 - getSumOfIncrements().
+int mdsx_batch_get_log_likelihood(mdsx_batch* b, int k, double* out) {
+    double s = 0.0;
+    int rc = mdsx_batch_get_sum_of_increments(b, k, &s);
+    if (rc) return rc;
+    const BatchInst& in = b->inst[k];
+    *out = 0.5 * (std::log(in.tau) - std::log(2.0 * M_PI)) * ((double)in.n * (in.n - 1) / 2.0) - s;
+    return MDSX_OK;
+}
+
+int mdsx_batch_get_log_likelihood_gradient(mdsx_batch* b, int k, double* out, size_t length) {
+    if (!b) return MDSX_EINVAL;
+    int rc = check_instance(b, k);
+    if (rc) return rc;
+    const BatchInst& in = b->inst[k];
+    if (!out || length != (size_t)in.n * in.p) return bfail(b, MDSX_EINVAL, "gradient buffer must hold N*P values");
+    Guard guard(b->device);
+    if ((rc = ensure_results(b))) return rc;
+    std::memcpy(out, b->h_results + 4 * b->inst.size() + in.grad_off, length * sizeof(double));
+    return MDSX_OK;
+}
+
+// Shape chosen for the group of embedding dimension p: rows per warp, CTAs per SM, grid.
+int mdsx_batch_group_shape(mdsx_batch* b, int p, int* rows_per_warp, int* ctas_per_sm, int* grid) {
+    if (!b) return MDSX_EINVAL;
+    Guard guard(b->device);
+    if (!b->planned) {
+        int rc = plan(b, b->forced.empty() ? nullptr : &b->forced);
+        if (rc) return rc;
+    }
+    for (const auto& g : b->groups)
+        if (g.p == p) {
+            if (rows_per_warp) *rows_per_warp = g.rw;
+            if (ctas_per_sm) *ctas_per_sm = g.ctas_per_sm;
+            if (grid) *grid = g.grid;
+            return MDSX_OK;
+        }
+    return bfail(b, MDSX_EINVAL, "no instance of that embedding dimension");
+}
+
+}  // extern "C"
+
+namespace {
+
+// Mean device time (microseconds) of one group's launch over `reps` launches.
+int time_group(mdsx_batch* b, const BatchGroup& g, int reps, double* us) {
+    const BatchArgs a = group_args(b, g);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BCUDA(b, cudaEventCreate(&e0));
+    BCUDA(b, cudaEventCreate(&e1));
+    cudaError_t ce = cudaSuccess;
+    for (int w = 0; w < 2 && ce == cudaSuccess; ++w) ce = mdsx::batch::launch(g.p, g.trunc, g.rw, a, b->stream);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e0, b->stream);
+    for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = mdsx::batch::launch(g.p, g.trunc, g.rw, a, b->stream);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e1, b->stream);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    BCUDA(b, ce);
+    int err = 0;
+    BCUDA(b, cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return bfail(b, MDSX_ETIMEOUT, "a bounded device wait timed out while tuning");
+    *us = 1e3 * ms / reps;
+    return MDSX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Test and tuning hook: fixes the shape (rows per warp, CTAs per SM) of the
+// group of embedding dimension p; rows_per_warp 0 removes the override.
+int mdsx_batch_force_shape(mdsx_batch* b, int p, int rows_per_warp, int ctas_per_sm) {
+    if (!b) return MDSX_EINVAL;
+    const std::pair<int, int> key{p, b->trunc ? 1 : 0};
+    if (rows_per_warp == 0) {
+        b->forced.erase(key);
+    } else {
+        if (!mdsx::batch::rw_built(p, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4)
+            return bfail(b, MDSX_EINVAL, "rows per warp not built for this dimension, or CTAs per SM outside 1..4");
+        b->forced[key] = {rows_per_warp, ctas_per_sm};
+    }
+    free_plan(b);
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+// Autotuner: times every built (rows per warp, CTAs per SM) candidate of each
+// group on this batch (`repetitions` launches each, after two warm-ups) and
+// caches the fastest per (P, N-bucket, truncation); later plans of any batch
+// in this process (and in others, through MDSX_TUNE_CACHE) use it. Writes the
+// number of candidates timed to *candidates when non-NULL.
+int mdsx_batch_tune(mdsx_batch* b, int repetitions, int* candidates) {
+    if (!b) return MDSX_EINVAL;
+    if (repetitions < 1) return bfail(b, MDSX_EINVAL, "repetitions must be >= 1");
+    Guard guard(b->device);
+    int rc = plan(b);
+    if (rc) return rc;
+    struct Key {
+        int p, trunc, bucket;
+    };
+    std::vector<Key> keys;
+    for (const auto& g : b->groups) {
+        double mean_n = 0.0;
+        for (int k : g.members) mean_n += b->inst[k].n;
+        keys.push_back({g.p, g.trunc ? 1 : 0, mdsx::batch::n_bucket(mean_n / g.members.size())});
+    }
+    int timed = 0;
+    std::map<std::pair<int, int>, std::pair<int, int>> best_shape;
+    std::map<std::pair<int, int>, double> best_us;
+    for (int rw : {1, 2, 4})
+        for (int ctas : {1, 2}) {
+            std::map<std::pair<int, int>, std::pair<int, int>> force;
+            bool any = false;
+            for (const auto& k : keys)
+                if (mdsx::batch::rw_built(k.p, rw)) {
+                    int occ = 0;
+                    size_t local = 0;
+                    if (mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local) != cudaSuccess || occ < ctas)
+                        continue;
+                    force[{k.p, k.trunc}] = {rw, ctas};
+                    any = true;
+                }
+            if (!any) continue;
+            if ((rc = plan(b, &force))) return rc;
+            if ((rc = upload_descriptors(b))) return rc;
+            for (const auto& g : b->groups) {
+                const std::pair<int, int> key{g.p, g.trunc ? 1 : 0};
+                auto f = force.find(key);
+                if (f == force.end() || g.rw != rw || g.ctas_per_sm != ctas) continue;
+                double us = 0.0;
+                if ((rc = time_group(b, g, repetitions, &us))) return rc;
+                ++timed;
+                if (!best_us.count(key) || us < best_us[key]) {
+                    best_us[key] = us;
+                    best_shape[key] = {rw, ctas};
+                }
+            }
+        }
+    {
+        std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
+        mdsx::batch::load_cache_locked();
+        for (const auto& k : keys) {
+            const std::pair<int, int> key{k.p, k.trunc};
+            if (!best_shape.count(key)) continue;
+            mdsx::batch::g_tune[{k.p, k.bucket, k.trunc}] = {best_shape[key].first, best_shape[key].second,
+                                                               best_us[key]};
+        }
+        mdsx::batch::save_cache_locked();
+    }
+    if (candidates) *candidates = timed;
+    free_plan(b);  // the next evaluation plans with the tuned shapes
+    b->results_known = false;
+    return MDSX_OK;
+}
+
+}  // extern "C"

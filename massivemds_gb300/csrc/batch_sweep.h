@@ -1,0 +1,30 @@
+// Host interface of the batched sweep kernels (batch_sweep_lo.cu: P 1..4,
+// batch_sweep_hi.cu: P 5..10; two translation units so they build in parallel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+#include "batch_kernel.cuh"
+
+namespace mdsx {
+namespace batch {
+
+// Rows per warp built for P: {1, 2, 4} for P <= 4, {1, 2} for P <= 8, {1} above.
+bool rw_built(int p, int rw);
+// Dynamic shared memory of one CTA.
+int smem_bytes(int p, int rw);
+// Resident CTAs per SM and local (spill) bytes per thread of the kernel.
+cudaError_t occupancy(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes);
+cudaError_t launch(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st);
+
+#define MDSX_BATCH_DECLARE(R)                                                                  \
+    cudaError_t occupancy_##R(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes); \
+    cudaError_t launch_##R(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st);
+MDSX_BATCH_DECLARE(lo)
+MDSX_BATCH_DECLARE(hi)
+#undef MDSX_BATCH_DECLARE
+
+}  // namespace batch
+}  // namespace mdsx

@@ -1,0 +1,40 @@
+// Batched sweep kernels for P = 5..10 (see batch_kernel.cuh).
+#include "batch_dispatch.cuh"
+
+namespace mdsx {
+namespace batch {
+
+cudaError_t launch_hi(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st) {
+#define FN launch_p
+#define ARGS trunc, a, st
+    switch (p) {
+        MDSX_BATCH_CASE(5)
+        MDSX_BATCH_CASE(6)
+        MDSX_BATCH_CASE(7)
+        MDSX_BATCH_CASE(8)
+        MDSX_BATCH_CASE(9)
+        MDSX_BATCH_CASE(10)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
+cudaError_t occupancy_hi(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes) {
+#define FN occupancy_p
+#define ARGS trunc, ctas_per_sm, local_bytes
+    switch (p) {
+        MDSX_BATCH_CASE(5)
+        MDSX_BATCH_CASE(6)
+        MDSX_BATCH_CASE(7)
+        MDSX_BATCH_CASE(8)
+        MDSX_BATCH_CASE(9)
+        MDSX_BATCH_CASE(10)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
+}  // namespace batch
+}  // namespace mdsx

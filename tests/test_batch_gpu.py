@@ -1,0 +1,147 @@
+"""GPU parity tests of the batched multi-instance engine (batch.cu,
+batch_kernel.cuh) against the oracle, instance by instance: every instance's
+sum of increments and gradient within 1e-5 relative of the FP64 oracle on its
+FP32-rounded delta (the FP32 bar of the single-instance engine), for uneven N,
+mixed P, every built tile shape, missing pairs, single-location updates and
+precision changes; plus determinism and the autotuner."""
+import numpy as np
+import pytest
+
+import oracle
+from massivemds_gb300 import Engine, flags as F
+from massivemds_gb300 import data as gen
+from massivemds_gb300.batch import Batch
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def _grad_rel(g, ref):
+    g = np.asarray(g).reshape(ref.shape)
+    return np.abs(g - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+def _problems(spec, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n, p in spec:
+        delta = gen.euclidean_delta(n, dim=10, seed=int(rng.integers(1 << 30))).astype(np.float32)
+        x = rng.standard_normal((n, p))
+        tau = float(rng.gamma(2.0, 1.0)) + 0.05
+        out.append((delta, x, tau))
+    return out
+
+
+def _fill(b, problems):
+    for delta, x, tau in problems:
+        k = b.add_instance(x.shape[1], x.shape[0])
+        b.setPairwiseData(k, delta)
+        b.updateLocations(k, -1, x)
+        b.setParameters(k, [tau])
+
+
+def _check(b, problems, trunc=True):
+    for k, (delta, x, tau) in enumerate(problems):
+        s_ref = oracle.sum_of_increments(delta, x, tau, trunc)
+        g_ref = oracle.gradient(delta, x, tau, trunc)
+        assert _rel(b.getSumOfIncrements(k), s_ref) < TOL, k
+        assert _grad_rel(b.getLogLikelihoodGradient(k), g_ref) < TOL, k
+
+
+SPEC = [(257, 2), (300, 3), (513, 6), (130, 2), (1024, 3), (777, 6), (64, 2), (999, 2)]
+
+
+def test_mixed_instances_match_oracle():
+    problems = _problems(SPEC, 1)
+    with Batch() as b:
+        _fill(b, problems)
+        _check(b, problems)
+        ll = b.getLogLikelihood(0)
+        delta, x, tau = problems[0]
+        assert _rel(ll, oracle.log_likelihood(oracle.sum_of_increments(delta, x, tau), x.shape[0], tau)) < TOL
+
+
+@pytest.mark.parametrize("p,rw,ctas", [(2, 1, 2), (2, 2, 1), (2, 4, 2), (3, 1, 1), (3, 2, 2), (3, 4, 1),
+                                       (6, 1, 2), (6, 2, 1)])
+def test_every_shape_matches_oracle(p, rw, ctas):
+    problems = _problems([(257, p), (640, p), (129, p), (1000, p)], 10 + rw)
+    with Batch() as b:
+        _fill(b, problems)
+        b.force_shape(p, rw, ctas)
+        assert b.group_shape(p)[:2] == (rw, ctas)
+        _check(b, problems)
+
+
+def test_without_truncation():
+    problems = _problems([(300, 2), (450, 3)], 3)
+    with Batch(flags=F.FLOAT) as b:
+        _fill(b, problems)
+        _check(b, problems, trunc=False)
+
+
+def test_missing_pairs():
+    problems = _problems([(300, 2), (260, 3)], 4)
+    d = problems[0][0].copy()
+    rng = np.random.default_rng(0)
+    i, j = rng.integers(0, 300, 40), rng.integers(0, 300, 40)
+    d[i, j] = np.nan
+    d[j, i] = np.nan
+    problems[0] = (d, problems[0][1], problems[0][2])
+    with Batch() as b:
+        _fill(b, problems)
+        _check(b, problems)
+
+
+def test_updates_are_lazy_and_local():
+    problems = _problems([(300, 2), (200, 6), (512, 3)], 5)
+    with Batch() as b:
+        _fill(b, problems)
+        _check(b, problems)
+        # one location of instance 1, the precision of instance 2
+        delta, x, tau = problems[1]
+        x = x.copy()
+        x[17] += 0.25
+        b.updateLocations(1, 17, x[17])
+        problems[1] = (delta, x, tau)
+        delta2, x2, _ = problems[2]
+        b.setParameters(2, [3.5])
+        problems[2] = (delta2, x2, 3.5)
+        _check(b, problems)
+
+
+def test_deterministic_and_same_as_single_engine():
+    problems = _problems([(700, 2), (333, 3)], 6)
+    with Batch() as b:
+        _fill(b, problems)
+        b.evaluate()
+        first = [b.getLogLikelihoodGradient(k).copy() for k in range(2)]
+        s1 = [b.getSumOfIncrements(k) for k in range(2)]
+        b.makeDirty()
+        b.evaluate()
+        assert [b.getSumOfIncrements(k) for k in range(2)] == s1
+        for k in range(2):
+            assert np.array_equal(b.getLogLikelihoodGradient(k), first[k])
+    for k, (delta, x, tau) in enumerate(problems):
+        e = Engine(x.shape[1], x.shape[0], F.FLOAT | F.LEFT_TRUNCATION)
+        e.setPairwiseData(delta)
+        e.updateLocations(-1, x)
+        e.setParameters([tau])
+        assert _rel(e.getSumOfIncrements(), s1[k]) < 1e-6
+        assert _grad_rel(e.getLogLikelihoodGradient(), first[k].reshape(x.shape)) < 1e-6
+        e.close()
+
+
+def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
+    monkeypatch.setenv("MDSX_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    problems = _problems([(800, 2), (600, 2), (500, 3), (900, 6)], 7)
+    with Batch() as b:
+        _fill(b, problems)
+        assert b.tune(repetitions=3) >= 3
+        for p in (2, 3, 6):
+            rw, ctas, grid = b.group_shape(p)
+            assert rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
+        _check(b, problems)
