@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kThreads, MDSX_F32_MIN_CTAS) batch_sweep_kerne
                     stage = kStages - 1;
                     phase ^= 1u;
                 }
-                mbar_wait_bounded(&full[stage], phase, a.err, kDevTimeoutFull);
+                mbar_wait_time_only(&full[stage], phase);
             }
         }
         return;

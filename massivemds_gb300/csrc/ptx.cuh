@@ -75,6 +75,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     }
 }
 
+// Waits for phase `parity` of `bar` for at most kWaitLimitNs whatever the
+// error word says: a thread that issued copies waits for them to land before
+// its CTA exits, also after another thread reported an error.
+__device__ __forceinline__ bool mbar_wait_time_only(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t start = global_timer_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_timer_ns() - start > kWaitLimitNs) return false;
+    return true;
+}
+
 // 2-D TMA tile load global -> shared, completing `bytes` on `bar`.
 // c0 is the innermost (column) coordinate in elements, c1 the row.
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {

@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                     phase ^= 1u;
                 }
                 // phase now holds the parity that stage's latest fill completes.
-                mbar_wait_bounded(&full[stage], phase, a.err, kDevTimeoutFull);
+                mbar_wait_time_only(&full[stage], phase);
             }
         }
         return;
