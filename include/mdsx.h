@@ -281,15 +281,19 @@ int mdsx_batch_evaluate(mdsx_batch* batch);
  * unused), d_gradients the instances' N*P gradients concatenated in instance
  * order; either may be NULL. */
 int mdsx_batch_evaluate_device(mdsx_batch* batch, double* d_sums, double* d_gradients);
-/* Autotuner: times every built (rows per warp, CTAs per SM) shape of each
- * dimension group on this batch and caches the fastest per (P, N-bucket =
- * floor(log2 mean N), truncation), in process and in the file named by the
- * environment variable MDSX_TUNE_CACHE. *candidates (may be NULL) = shapes timed. */
+/* Shapes: schedule 0 = stream-K over (row block x 128 columns) units of all
+ * instances, 1 = queue of whole row blocks (largest instance first, each CTA
+ * owning the row blocks it takes); rows per warp (1, 2, 4 as built for P);
+ * CTAs per SM. Autotuner: times every built shape of each dimension group on
+ * this batch and caches the fastest per (P, N-bucket = floor(log2 mean N),
+ * truncation), in process and in the file named by the environment variable
+ * MDSX_TUNE_CACHE. *candidates (may be NULL) = shapes timed. */
 int mdsx_batch_tune(mdsx_batch* batch, int repetitions, int* candidates);
 /* Shape in use for dimension p (plans the batch if needed). */
-int mdsx_batch_group_shape(mdsx_batch* batch, int p, int* rows_per_warp, int* ctas_per_sm, int* grid);
+int mdsx_batch_group_shape(mdsx_batch* batch, int p, int* schedule, int* rows_per_warp, int* ctas_per_sm,
+                           int* grid);
 /* Fixes the shape of dimension p's group (rows_per_warp 0 removes it). */
-int mdsx_batch_force_shape(mdsx_batch* batch, int p, int rows_per_warp, int ctas_per_sm);
+int mdsx_batch_force_shape(mdsx_batch* batch, int p, int schedule, int rows_per_warp, int ctas_per_sm);
 
 /* ---- Allocation-free variant (no counterpart in the reference) ----
  * For callers that cannot allocate device memory: hosts whose GPU memory is

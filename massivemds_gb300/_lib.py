@@ -77,8 +77,8 @@ SIGNATURES = {
     "mdsx_batch_evaluate": (_i, [_vp]),
     "mdsx_batch_evaluate_device": (_i, [_vp, _vp, _vp]),
     "mdsx_batch_tune": (_i, [_vp, _i, _ip]),
-    "mdsx_batch_group_shape": (_i, [_vp, _i, _ip, _ip, _ip]),
-    "mdsx_batch_force_shape": (_i, [_vp, _i, _i, _i]),
+    "mdsx_batch_group_shape": (_i, [_vp, _i, _ip, _ip, _ip, _ip]),
+    "mdsx_batch_force_shape": (_i, [_vp, _i, _i, _i, _i]),
     "mdsx_test_gemm_bf16": (_i, [_i, _i, _i, _i, _i, ctypes.POINTER(ctypes.c_ushort),
                                  ctypes.POINTER(ctypes.c_ushort), _fp]),
 }

@@ -6,8 +6,9 @@ src/jni/dr_inference_multidimensionalscaling_NativeMDSSingleton.cpp:10-100).
 ``Batch`` keeps that call surface (initialize -> add_instance, then
 updateLocations / setPairwiseData / setParameters / getSumOfIncrements /
 getLogLikelihoodGradient / makeDirty by index) but evaluates all instances
-together: one persistent stream-K launch per embedding dimension on one GPU,
-captured as a CUDA graph, with shapes from the autotuner (``tune``).
+together: one persistent launch per embedding dimension on one GPU, captured
+as a CUDA graph, with the schedule (stream-K units or a queue of whole row
+blocks) and tile shape from the autotuner (``tune``).
 """
 from __future__ import annotations
 
@@ -121,11 +122,14 @@ class Batch:
         self._check(self._lib.mdsx_batch_tune(self._h, int(repetitions), ctypes.byref(c)))
         return c.value
 
-    def group_shape(self, p: int) -> tuple[int, int, int]:
-        rw, ctas, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        self._check(self._lib.mdsx_batch_group_shape(self._h, int(p), ctypes.byref(rw), ctypes.byref(ctas),
-                                                     ctypes.byref(grid)))
-        return rw.value, ctas.value, grid.value
+    def group_shape(self, p: int) -> tuple[int, int, int, int]:
+        """(schedule, rows per warp, CTAs per SM, grid) of dimension p's group;
+        schedule 0 = stream-K units, 1 = row-block queue."""
+        sc, rw, ctas, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self._lib.mdsx_batch_group_shape(self._h, int(p), ctypes.byref(sc), ctypes.byref(rw),
+                                                     ctypes.byref(ctas), ctypes.byref(grid)))
+        return sc.value, rw.value, ctas.value, grid.value
 
-    def force_shape(self, p: int, rows_per_warp: int, ctas_per_sm: int = 2) -> None:
-        self._check(self._lib.mdsx_batch_force_shape(self._h, int(p), int(rows_per_warp), int(ctas_per_sm)))
+    def force_shape(self, p: int, rows_per_warp: int, ctas_per_sm: int = 2, schedule: int = 1) -> None:
+        self._check(self._lib.mdsx_batch_force_shape(self._h, int(p), int(schedule), int(rows_per_warp),
+                                                     int(ctas_per_sm)))

@@ -8,7 +8,7 @@ instance. Algorithmic bytes per batch evaluation: sum_k N_k^2 * 4.
 
 Arms, each timed with CUDA events after warm-up, inputs resident on the GPU:
   batched   mdsx_batch_evaluate_device: one graph launch (one persistent
-            stream-K kernel per dimension group);
+            kernel per dimension group, schedule and shape from the tuner);
   engines   64 single-instance engines, mdsx_evaluate_device on each engine's
             own stream, all enqueued before one synchronisation (engines
             overlap on the GPU: the strongest use of separate engines);
@@ -159,7 +159,8 @@ def main(argv=None):
         "speedup_vs_engines": t_engines / t_batch,
         "speedup_vs_engines_sync": t_sync / t_batch,
         "tuned_candidates": candidates,
-        "shapes": {str(p): {"rows_per_warp": s[0], "ctas_per_sm": s[1], "grid": s[2]} for p, s in shapes.items()},
+        "shapes": {str(p): {"schedule": ("stream-K", "row-block queue")[s[0]], "rows_per_warp": s[1],
+                            "ctas_per_sm": s[2], "grid": s[3]} for p, s in shapes.items()},
         "setup_seconds": setup_s,
     }
     print(json.dumps(out))

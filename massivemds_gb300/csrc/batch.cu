@@ -6,12 +6,14 @@
 // updateLocations, getSumOfIncrements, getLogLikelihoodGradient,
 // setPairwiseData, setParameters, makeDirty), by one object that owns every
 // instance's data on one GPU and evaluates all of them with one persistent
-// stream-K launch per (P, truncation) group (batch_kernel.cuh), the launches
-// captured once as a CUDA graph. Results of all instances come back in one
+// launch per (P, truncation) group, the launches captured once as a CUDA
+// graph. Two schedules: stream-K over (row block x 128 columns) units of all
+// instances (batch_kernel.cuh), and a queue of whole row blocks taken
+// dynamically, largest instance first (batch_queue.cuh). Results of all instances come back in one
 // device-to-host copy. Instance calls keep the reference's names and lazy
 // semantics: a getter evaluates the batch when any instance changed.
 //
-// Tile shapes (rows per warp, CTAs per SM) come from an autotuner that times
+// Shapes (schedule, rows per warp, CTAs per SM) come from an autotuner that times
 // the candidates on the batch itself and caches the winner per (P, N-bucket,
 // truncation), in process and, when MDSX_TUNE_CACHE names a file, on disk.
 #include <cuda.h>
@@ -55,6 +57,14 @@ cudaError_t launch(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t s
     return p <= 4 ? launch_lo(p, trunc, rw, a, st) : launch_hi(p, trunc, rw, a, st);
 }
 
+cudaError_t occupancy_queue(int p, bool trunc, int rw, int* ctas) {
+    return p <= 4 ? occupancy_queue_lo(p, trunc, rw, ctas) : occupancy_queue_hi(p, trunc, rw, ctas);
+}
+
+cudaError_t launch_queue(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st) {
+    return p <= 4 ? launch_queue_lo(p, trunc, rw, a, grid, st) : launch_queue_hi(p, trunc, rw, a, grid, st);
+}
+
 namespace {
 
 // ------------------------------------------------------------ tuning cache
@@ -64,7 +74,7 @@ struct TuneKey {
     bool operator<(const TuneKey& o) const { return std::tie(p, bucket, trunc) < std::tie(o.p, o.bucket, o.trunc); }
 };
 struct TuneValue {
-    int rw, ctas_per_sm;
+    int schedule, rw, ctas_per_sm;  // schedule 0: stream-K (batch_kernel.cuh), 1: row-block queue (batch_queue.cuh)
     double us;
 };
 
@@ -82,10 +92,10 @@ void load_cache_locked() {
     if (!path) return;
     FILE* f = std::fopen(path, "r");
     if (!f) return;
-    int p, b, t, rw, c;
+    int p, b, t, sc, rw, c;
     double us;
-    while (std::fscanf(f, "%d %d %d %d %d %lf", &p, &b, &t, &rw, &c, &us) == 6)
-        if (rw_built(p, rw) && c >= 1 && c <= 4) g_tune[{p, b, t}] = {rw, c, us};
+    while (std::fscanf(f, "%d %d %d %d %d %d %lf", &p, &b, &t, &sc, &rw, &c, &us) == 7)
+        if (rw_built(p, rw) && c >= 1 && c <= 4 && (sc == 0 || sc == 1)) g_tune[{p, b, t}] = {sc, rw, c, us};
     std::fclose(f);
 }
 
@@ -95,8 +105,8 @@ void save_cache_locked() {
     FILE* f = std::fopen(path, "w");
     if (!f) return;
     for (const auto& kv : g_tune)
-        std::fprintf(f, "%d %d %d %d %d %.3f\n", kv.first.p, kv.first.bucket, kv.first.trunc, kv.second.rw,
-                     kv.second.ctas_per_sm, kv.second.us);
+        std::fprintf(f, "%d %d %d %d %d %d %.3f\n", kv.first.p, kv.first.bucket, kv.first.trunc, kv.second.schedule,
+                     kv.second.rw, kv.second.ctas_per_sm, kv.second.us);
     std::fclose(f);
 }
 
@@ -130,7 +140,7 @@ struct BatchInst {
     bool data_set = false;
     float* d_delta = nullptr;  // [n][ld]
     long long ld = 0;
-    float* d_x = nullptr;      // SoA [p][x_ld]
+    float* d_x = nullptr;      // SoA [p + 1][x_ld]; row p: missing-row flags
     int x_ld = 0;
     double* d_xin = nullptr;   // row-major [n][p] staging
     // plan-dependent
@@ -140,18 +150,30 @@ struct BatchInst {
     double* d_lpart = nullptr;
     double* d_lrow = nullptr;
     unsigned* d_counts = nullptr;  // [R] row-block counters + [1] done counter
+    double* d_qlpart = nullptr;    // queue schedule: [R][warps][2] likelihood partials
+    unsigned* d_qdone = nullptr;   // queue schedule: row blocks finished
     long long grad_off = 0;        // offset (doubles) in the concatenated gradients
+};
+
+struct Shape {
+    int schedule = 1, rw = 0, ctas = 0;
 };
 
 struct BatchGroup {
     int p = 0;
     bool trunc = false;
-    int rw = 0, ctas_per_sm = 0;
+    int schedule = 1, rw = 0, ctas_per_sm = 0;
     std::vector<int> members;
     long long n_units = 0;
     int grid = 0;
     std::vector<mdsx::batch::BatchInstance> h_desc;
     mdsx::batch::BatchInstance* d_desc = nullptr;
+    // queue schedule
+    std::vector<int> order;  // members, largest N first (queue item order)
+    std::vector<mdsx::batch::QueueInstance> h_qdesc;
+    mdsx::batch::QueueInstance* d_qdesc = nullptr;
+    unsigned long long* d_next = nullptr;
+    long long n_items = 0;
     double work = 0.0;  // modelled cost: sum of N^2 x (16 + 3P) instructions per pair
 };
 
@@ -174,7 +196,7 @@ struct mdsx_batch {
     std::vector<cudaStream_t> aux;     // one branch stream per dimension group (graph capture)
     std::vector<cudaEvent_t> aux_ev;   // [0] fork, [1 + g] join of group g
     long long evaluations = 0;
-    std::map<std::pair<int, int>, std::pair<int, int>> forced;  // (p, trunc) -> (rw, ctas per SM)
+    std::map<std::pair<int, int>, Shape> forced;  // (p, trunc) -> shape
     std::string last_error;
 };
 
@@ -209,6 +231,10 @@ struct Guard {
 };
 
 void free_plan_scratch(BatchInst& in) {
+    cudaFree(in.d_qlpart);
+    cudaFree(in.d_qdone);
+    in.d_qlpart = nullptr;
+    in.d_qdone = nullptr;
     cudaFree(in.d_row_nan);
     cudaFree(in.d_gpart);
     cudaFree(in.d_lpart);
@@ -231,7 +257,11 @@ void drop_graph(mdsx_batch* b) {
 
 void free_plan(mdsx_batch* b) {
     drop_graph(b);
-    for (auto& g : b->groups) cudaFree(g.d_desc);
+    for (auto& g : b->groups) {
+        cudaFree(g.d_desc);
+        cudaFree(g.d_qdesc);
+        cudaFree(g.d_next);
+    }
     b->groups.clear();
     for (auto& in : b->inst) free_plan_scratch(in);
     cudaFree(b->d_grad_all);
@@ -259,7 +289,8 @@ int make_tmap(mdsx_batch* b, CUtensorMap* map, void* base, long long cols, long 
 }
 
 // Precision constants of one instance (the single-instance engine's make_args).
-void set_precision_constants(BatchInstance& d, double tau) {
+template <typename D>
+void set_precision_constants(D& d, double tau) {
     const double s = std::sqrt(tau);
     d.tau = tau;
     d.k_e = (float)(-0.5 * tau * 1.4426950408889634074);
@@ -272,9 +303,34 @@ void set_precision_constants(BatchInstance& d, double tau) {
     d.ts2 = (float)(mdsx::kTailS2 / s);
 }
 
+// Missing-row flags into row P of the SoA location array (read by the queue
+// schedule with the row block's locations): 1 for rows whose delta row has a NaN.
+__global__ void flag_rows_kernel(const int* __restrict__ row_nan, int n, float* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) flags[i] = row_nan[i] ? 1.0f : 0.0f;
+}
+
+// Shape of a group: the override, else the tuning cache, else the default
+// (row-block queue, the single-instance rows per warp, full occupancy).
+Shape group_shape(const mdsx_batch* b, int p, double mean_n, const std::map<std::pair<int, int>, Shape>* force) {
+    Shape sh;
+    sh.rw = mdsx::batch::default_rw(p);
+    {
+        std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
+        mdsx::batch::load_cache_locked();
+        auto it = mdsx::batch::g_tune.find({p, mdsx::batch::n_bucket(mean_n), b->trunc ? 1 : 0});
+        if (it != mdsx::batch::g_tune.end()) sh = {it->second.schedule, it->second.rw, it->second.ctas_per_sm};
+    }
+    if (force) {
+        auto it = force->find({p, b->trunc ? 1 : 0});
+        if (it != force->end()) sh = it->second;
+    }
+    return sh;
+}
+
 // Builds the groups, scratch, descriptors and result buffers. `force` maps a
-// group key (p, trunc) to a shape (rw, ctas per SM) that overrides the cache.
-int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>* force = nullptr) {
+// group key (p, trunc) to a shape that overrides the cache.
+int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = nullptr) {
     if (b->inst.empty()) return bfail(b, MDSX_ESTATE, "batch has no instances");
     for (size_t k = 0; k < b->inst.size(); ++k) {
         if (!b->inst[k].data_set) return bfail(b, MDSX_ESTATE, "instance " + std::to_string(k) + ": no pairwise data");
@@ -282,15 +338,18 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>
     }
     free_plan(b);
     cudaStream_t st = b->stream;
-    // groups by P (one truncation mode per batch)
+    // gradients concatenated in instance order
+    long long grad_off = 0;
+    for (auto& in : b->inst) {
+        in.grad_off = grad_off;
+        grad_off += (long long)in.n * in.p;
+    }
+    // groups by P (one truncation mode per batch); they run concurrently as graph branches
     std::map<int, std::vector<int>> by_p;
     for (size_t k = 0; k < b->inst.size(); ++k) by_p[b->inst[k].p].push_back((int)k);
-    // Groups run concurrently (graph branches), each on a share of the
-    // machine proportional to its modelled cost.
     double total_work = 0.0;
     for (const auto& in : b->inst) total_work += (double)in.n * in.n * (16.0 + 3.0 * in.p);
     const bool concurrent = by_p.size() > 1;
-    long long grad_off = 0;
     for (auto& kv : by_p) {
         BatchGroup g;
         g.p = kv.first;
@@ -299,86 +358,105 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>
         double mean_n = 0.0;
         for (int k : g.members) mean_n += b->inst[k].n;
         mean_n /= g.members.size();
-        int rw = mdsx::batch::default_rw(g.p), ctas = 0;
-        {
-            std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
-            mdsx::batch::load_cache_locked();
-            auto it = mdsx::batch::g_tune.find({g.p, mdsx::batch::n_bucket(mean_n), g.trunc ? 1 : 0});
-            if (it != mdsx::batch::g_tune.end()) {
-                rw = it->second.rw;
-                ctas = it->second.ctas_per_sm;
-            }
-        }
-        if (force) {
-            auto it = force->find({g.p, g.trunc ? 1 : 0});
-            if (it != force->end()) {
-                rw = it->second.first;
-                ctas = it->second.second;
-            }
-        }
+        const Shape sh = group_shape(b, g.p, mean_n, force);
         int occ = 0;
         size_t local = 0;
-        BCUDA(b, mdsx::batch::occupancy(g.p, g.trunc, rw, &occ, &local));
+        if (sh.schedule == 0)
+            BCUDA(b, mdsx::batch::occupancy(g.p, g.trunc, sh.rw, &occ, &local));
+        else
+            BCUDA(b, mdsx::batch::occupancy_queue(g.p, g.trunc, sh.rw, &occ));
         if (occ < 1) return bfail(b, MDSX_ECUDA, "batched sweep kernel cannot be resident");
-        g.rw = rw;
-        g.ctas_per_sm = ctas >= 1 ? std::min(ctas, occ) : occ;
-        const int rb = 8 * rw;
-        // global units
-        for (int k : g.members) {
-            BatchInst& in = b->inst[k];
-            BatchInstance d{};
-            const int nrb = (in.n + rb - 1) / rb;
-            const int spr = (in.n + mdsx::kStepCols - 1) / mdsx::kStepCols;
-            d.unit_begin = g.n_units;
-            d.n = in.n;
-            d.n_row_blocks = nrb;
-            d.steps_per_row = spr;
-            d.x_ld = in.x_ld;
-            d.truncation = g.trunc ? 1 : 0;
-            set_precision_constants(d, in.tau);
-            g.n_units += (long long)nrb * spr;
-            g.h_desc.push_back(d);
-        }
+        g.schedule = sh.schedule;
+        g.rw = sh.rw;
+        g.ctas_per_sm = sh.ctas >= 1 ? std::min(sh.ctas, occ) : occ;
+        const int rb = 8 * g.rw;
         g.work = 0.0;
         for (int k : g.members) g.work += (double)b->inst[k].n * b->inst[k].n * (16.0 + 3.0 * g.p);
-        long long slots = (long long)b->sm_count * g.ctas_per_sm;
-        if (concurrent) slots = std::max<long long>(1, std::llround(slots * g.work / total_work));
-        g.grid = (int)std::min<long long>(g.n_units, slots);
-        // per-instance slots, scratch, tensor maps
-        for (size_t m = 0; m < g.members.size(); ++m) {
-            BatchInst& in = b->inst[g.members[m]];
-            BatchInstance& d = g.h_desc[m];
-            int max_slots = 1;
-            for (int r = 0; r < d.n_row_blocks; ++r) {
-                const long long u0 = d.unit_begin + (long long)r * d.steps_per_row, u1 = u0 + d.steps_per_row - 1;
-                max_slots = std::max(max_slots, mdsx::cta_of_unit(u1, g.n_units, g.grid) -
-                                                    mdsx::cta_of_unit(u0, g.n_units, g.grid) + 1);
-            }
-            d.max_slots = max_slots;
-            in.rows_padded = d.n_row_blocks * rb;
-            in.n_row_blocks = d.n_row_blocks;
+        // per instance: row blocks, missing-row marks and flags
+        for (int k : g.members) {
+            BatchInst& in = b->inst[k];
+            in.n_row_blocks = (in.n + rb - 1) / rb;
+            in.rows_padded = in.n_row_blocks * rb;
             BCUDA(b, cudaMalloc(&in.d_row_nan, (size_t)in.rows_padded * sizeof(int)));
             BCUDA(b, mdsx::mark_nan_rows(in.d_delta, true, in.n, in.ld, in.d_row_nan, in.rows_padded, st));
-            BCUDA(b, cudaMalloc(&in.d_gpart, (size_t)d.n_row_blocks * max_slots * rb * g.p * sizeof(float)));
-            BCUDA(b, cudaMalloc(&in.d_lpart,
-                                (size_t)d.n_row_blocks * max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
-            BCUDA(b, cudaMalloc(&in.d_lrow, (size_t)d.n_row_blocks * 2 * sizeof(double)));
-            BCUDA(b, cudaMalloc(&in.d_counts, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned)));
-            BCUDA(b, cudaMemsetAsync(in.d_counts, 0, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned), st));
-            int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
-            if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p, in.x_ld, mdsx::kStepCols, g.p);
-            if (rc) return rc;
-            d.x = in.d_x;
-            d.row_nan = in.d_row_nan;
-            d.gpart = in.d_gpart;
-            d.lpart = in.d_lpart;
-            d.lrow = in.d_lrow;
-            d.rb_count = in.d_counts;
-            d.done_count = in.d_counts + d.n_row_blocks;
-            in.grad_off = grad_off;
-            grad_off += (long long)in.n * in.p;
+            flag_rows_kernel<<<(in.n + 255) / 256, 256, 0, st>>>(in.d_row_nan, in.n, in.d_x + (size_t)g.p * in.x_ld);
+            BCUDA(b, cudaGetLastError());
         }
-        BCUDA(b, cudaMalloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
+        if (g.schedule == 0) {
+            // stream-K: global units, slots, scratch
+            for (int k : g.members) {
+                BatchInst& in = b->inst[k];
+                BatchInstance d{};
+                d.unit_begin = g.n_units;
+                d.n = in.n;
+                d.n_row_blocks = in.n_row_blocks;
+                d.steps_per_row = (in.n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+                d.x_ld = in.x_ld;
+                d.truncation = g.trunc ? 1 : 0;
+                set_precision_constants(d, in.tau);
+                g.n_units += (long long)d.n_row_blocks * d.steps_per_row;
+                g.h_desc.push_back(d);
+            }
+            long long slots = (long long)b->sm_count * g.ctas_per_sm;
+            if (concurrent) slots = std::max<long long>(1, std::llround(slots * g.work / total_work));
+            g.grid = (int)std::min<long long>(g.n_units, slots);
+            for (size_t m = 0; m < g.members.size(); ++m) {
+                BatchInst& in = b->inst[g.members[m]];
+                BatchInstance& d = g.h_desc[m];
+                int max_slots = 1;
+                for (int r = 0; r < d.n_row_blocks; ++r) {
+                    const long long u0 = d.unit_begin + (long long)r * d.steps_per_row, u1 = u0 + d.steps_per_row - 1;
+                    max_slots = std::max(max_slots, mdsx::cta_of_unit(u1, g.n_units, g.grid) -
+                                                        mdsx::cta_of_unit(u0, g.n_units, g.grid) + 1);
+                }
+                d.max_slots = max_slots;
+                BCUDA(b, cudaMalloc(&in.d_gpart, (size_t)d.n_row_blocks * max_slots * rb * g.p * sizeof(float)));
+                BCUDA(b, cudaMalloc(&in.d_lpart,
+                                    (size_t)d.n_row_blocks * max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
+                BCUDA(b, cudaMalloc(&in.d_lrow, (size_t)d.n_row_blocks * 2 * sizeof(double)));
+                BCUDA(b, cudaMalloc(&in.d_counts, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned)));
+                BCUDA(b, cudaMemsetAsync(in.d_counts, 0, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned), st));
+                int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
+                if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p, in.x_ld, mdsx::kStepCols, g.p);
+                if (rc) return rc;
+                d.x = in.d_x;
+                d.row_nan = in.d_row_nan;
+                d.gpart = in.d_gpart;
+                d.lpart = in.d_lpart;
+                d.lrow = in.d_lrow;
+                d.rb_count = in.d_counts;
+                d.done_count = in.d_counts + d.n_row_blocks;
+            }
+            BCUDA(b, cudaMalloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
+        } else {
+            // row-block queue: items ordered largest instance first
+            g.order = g.members;
+            std::stable_sort(g.order.begin(), g.order.end(),
+                             [&](int x, int y) { return b->inst[x].n > b->inst[y].n; });
+            for (int k : g.order) {
+                BatchInst& in = b->inst[k];
+                mdsx::batch::QueueInstance d{};
+                d.n = in.n;
+                d.n_row_blocks = in.n_row_blocks;
+                d.steps_per_row = (in.n + mdsx::kStepCols - 1) / mdsx::kStepCols;
+                d.truncation = g.trunc ? 1 : 0;
+                d.item_begin = g.n_items;
+                set_precision_constants(d, in.tau);
+                g.n_items += in.n_row_blocks;
+                BCUDA(b, cudaMalloc(&in.d_qlpart, (size_t)in.n_row_blocks * mdsx::kConsumerWarps * 2 * sizeof(double)));
+                BCUDA(b, cudaMalloc(&in.d_qdone, sizeof(unsigned)));
+                BCUDA(b, cudaMemsetAsync(in.d_qdone, 0, sizeof(unsigned), st));
+                int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
+                if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p + 1, in.x_ld, mdsx::kStepCols, g.p + 1);
+                if (rc) return rc;
+                d.lpart = in.d_qlpart;
+                d.done_count = in.d_qdone;
+                g.h_qdesc.push_back(d);
+            }
+            g.grid = (int)std::max<long long>(1, std::min<long long>(g.n_items, (long long)b->sm_count * g.ctas_per_sm));
+            BCUDA(b, cudaMalloc(&g.d_qdesc, g.h_qdesc.size() * sizeof(mdsx::batch::QueueInstance)));
+            BCUDA(b, cudaMalloc(&g.d_next, sizeof(unsigned long long)));
+        }
         b->groups.push_back(std::move(g));
     }
     b->grad_total = grad_off;
@@ -388,12 +466,18 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>
     BCUDA(b, cudaMemsetAsync(b->d_sums_all, 0, count * 4 * sizeof(double), st));
     BCUDA(b, cudaMallocHost(&b->h_results, (count * 4 + (size_t)grad_off) * sizeof(double)));
     // output pointers (instance order in the sums array is the instance index)
-    for (auto& g : b->groups)
-        for (size_t m = 0; m < g.members.size(); ++m) {
+    for (auto& g : b->groups) {
+        for (size_t m = 0; m < g.h_desc.size(); ++m) {
             const int k = g.members[m];
             g.h_desc[m].grad_out = b->d_grad_all + b->inst[k].grad_off;
             g.h_desc[m].sums_out = b->d_sums_all + 4 * (size_t)k;
         }
+        for (size_t m = 0; m < g.h_qdesc.size(); ++m) {
+            const int k = g.order[m];
+            g.h_qdesc[m].grad_out = b->d_grad_all + b->inst[k].grad_off;
+            g.h_qdesc[m].sums_out = b->d_sums_all + 4 * (size_t)k;
+        }
+    }
     while (b->aux.size() < b->groups.size()) {  // branch streams for concurrent groups (created outside capture)
         cudaStream_t bs = nullptr;
         BCUDA(b, cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
@@ -412,9 +496,14 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, std::pair<int, int>>
 }
 
 int upload_descriptors(mdsx_batch* b) {
-    for (auto& g : b->groups)
-        BCUDA(b, cudaMemcpyAsync(g.d_desc, g.h_desc.data(), g.h_desc.size() * sizeof(BatchInstance),
-                                 cudaMemcpyHostToDevice, b->stream));
+    for (auto& g : b->groups) {
+        if (!g.h_desc.empty())
+            BCUDA(b, cudaMemcpyAsync(g.d_desc, g.h_desc.data(), g.h_desc.size() * sizeof(BatchInstance),
+                                     cudaMemcpyHostToDevice, b->stream));
+        if (!g.h_qdesc.empty())
+            BCUDA(b, cudaMemcpyAsync(g.d_qdesc, g.h_qdesc.data(), g.h_qdesc.size() * sizeof(mdsx::batch::QueueInstance),
+                                     cudaMemcpyHostToDevice, b->stream));
+    }
     BCUDA(b, cudaStreamSynchronize(b->stream));  // the host descriptors may change after return
     b->desc_dirty = false;
     return MDSX_OK;
@@ -430,21 +519,34 @@ BatchArgs group_args(const mdsx_batch* b, const BatchGroup& g) {
     return a;
 }
 
+// One group's launch on stream st (the queue schedule first resets its counter).
+int launch_group(mdsx_batch* b, const BatchGroup& g, cudaStream_t st) {
+    if (g.schedule == 0) {
+        BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), st));
+        return MDSX_OK;
+    }
+    mdsx::batch::QueueArgs a{};
+    a.inst = g.d_qdesc;
+    a.count = (int)g.h_qdesc.size();
+    a.n_items = g.n_items;
+    a.next = g.d_next;
+    a.err = b->d_err;
+    BCUDA(b, cudaMemsetAsync(g.d_next, 0, sizeof(unsigned long long), st));
+    BCUDA(b, mdsx::batch::launch_queue(g.p, g.trunc, g.rw, a, g.grid, st));
+    return MDSX_OK;
+}
+
 // The group launches: one group on the batch stream, several as concurrent
 // branches (fork from and join back to the batch stream).
 int enqueue_groups(mdsx_batch* b) {
-    if (b->groups.size() == 1) {
-        const BatchGroup& g = b->groups[0];
-        BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), b->stream));
-        return MDSX_OK;
-    }
+    if (b->groups.size() == 1) return launch_group(b, b->groups[0], b->stream);
     if (b->aux.size() < b->groups.size() || b->aux_ev.size() < b->groups.size() + 1)
         return bfail(b, MDSX_ESTATE, "branch streams missing (plan)");
     BCUDA(b, cudaEventRecord(b->aux_ev[0], b->stream));
     for (size_t i = 0; i < b->groups.size(); ++i) {
-        const BatchGroup& g = b->groups[i];
         BCUDA(b, cudaStreamWaitEvent(b->aux[i], b->aux_ev[0], 0));
-        BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), b->aux[i]));
+        const int rc = launch_group(b, b->groups[i], b->aux[i]);
+        if (rc) return rc;
         BCUDA(b, cudaEventRecord(b->aux_ev[1 + i], b->aux[i]));
         BCUDA(b, cudaStreamWaitEvent(b->stream, b->aux_ev[1 + i], 0));
     }
@@ -499,6 +601,8 @@ int ensure_results(mdsx_batch* b) {
         for (auto& in : b->inst)
             if (in.d_counts)
                 cudaMemsetAsync(in.d_counts, 0, ((size_t)in.n_row_blocks + 1) * sizeof(unsigned), b->stream);
+        for (auto& in : b->inst)
+            if (in.d_qdone) cudaMemsetAsync(in.d_qdone, 0, sizeof(unsigned), b->stream);
         cudaStreamSynchronize(b->stream);
         return bfail(b, MDSX_ETIMEOUT, "a bounded device wait in the batched sweep timed out");
     }
@@ -574,7 +678,7 @@ int mdsx_batch_add_instance(mdsx_batch* b, int embedding_dimension, int location
     in.n = location_count;
     in.ld = mdsx::batch::round_up(in.n, 4);
     in.x_ld = (int)mdsx::batch::round_up(in.n, mdsx::kStepCols);
-    const size_t xb = (size_t)in.p * in.x_ld * sizeof(float);
+    const size_t xb = (size_t)(in.p + 1) * in.x_ld * sizeof(float);  // row P: missing-row flags
     if (cudaMalloc(&in.d_delta, (size_t)in.n * in.ld * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&in.d_x, xb) != cudaSuccess ||
         cudaMalloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
@@ -634,9 +738,12 @@ int mdsx_batch_set_parameters(mdsx_batch* b, int k, const double* parameters, si
     if (!parameters || length < 1 || !(parameters[0] > 0.0) || !std::isfinite(parameters[0]))
         return bfail(b, MDSX_EINVAL, "precision must be finite and > 0");
     b->inst[k].tau = parameters[0];
-    for (auto& g : b->groups)
-        for (size_t m = 0; m < g.members.size(); ++m)
+    for (auto& g : b->groups) {
+        for (size_t m = 0; m < g.h_desc.size(); ++m)
             if (g.members[m] == k) set_precision_constants(g.h_desc[m], parameters[0]);
+        for (size_t m = 0; m < g.h_qdesc.size(); ++m)
+            if (g.order[m] == k) set_precision_constants(g.h_qdesc[m], parameters[0]);
+    }
     b->desc_dirty = true;
     b->results_known = false;
     return MDSX_OK;
@@ -734,7 +841,7 @@ int mdsx_batch_get_log_likelihood_gradient(mdsx_batch* b, int k, double* out, si
 }
 
 // Shape chosen for the group of embedding dimension p: rows per warp, CTAs per SM, grid.
-int mdsx_batch_group_shape(mdsx_batch* b, int p, int* rows_per_warp, int* ctas_per_sm, int* grid) {
+int mdsx_batch_group_shape(mdsx_batch* b, int p, int* schedule, int* rows_per_warp, int* ctas_per_sm, int* grid) {
     if (!b) return MDSX_EINVAL;
     Guard guard(b->device);
     if (!b->planned) {
@@ -743,6 +850,7 @@ int mdsx_batch_group_shape(mdsx_batch* b, int p, int* rows_per_warp, int* ctas_p
     }
     for (const auto& g : b->groups)
         if (g.p == p) {
+            if (schedule) *schedule = g.schedule;
             if (rows_per_warp) *rows_per_warp = g.rw;
             if (ctas_per_sm) *ctas_per_sm = g.ctas_per_sm;
             if (grid) *grid = g.grid;
@@ -757,21 +865,20 @@ namespace {
 
 // Mean device time (microseconds) of one group's launch over `reps` launches.
 int time_group(mdsx_batch* b, const BatchGroup& g, int reps, double* us) {
-    const BatchArgs a = group_args(b, g);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     BCUDA(b, cudaEventCreate(&e0));
     BCUDA(b, cudaEventCreate(&e1));
-    cudaError_t ce = cudaSuccess;
-    for (int w = 0; w < 2 && ce == cudaSuccess; ++w) ce = mdsx::batch::launch(g.p, g.trunc, g.rw, a, b->stream);
-    if (ce == cudaSuccess) ce = cudaEventRecord(e0, b->stream);
-    for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = mdsx::batch::launch(g.p, g.trunc, g.rw, a, b->stream);
-    if (ce == cudaSuccess) ce = cudaEventRecord(e1, b->stream);
-    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    int rc = MDSX_OK;
+    for (int w = 0; w < 2 && !rc; ++w) rc = launch_group(b, g, b->stream);
+    if (!rc && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = bfail(b, MDSX_ECUDA, "event record");
+    for (int r = 0; r < reps && !rc; ++r) rc = launch_group(b, g, b->stream);
     float ms = 0.f;
-    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+    if (!rc && (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+        rc = bfail(b, MDSX_ECUDA, "timing events failed");
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    BCUDA(b, ce);
+    if (rc) return rc;
     int err = 0;
     BCUDA(b, cudaMemcpy(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return bfail(b, MDSX_ETIMEOUT, "a bounded device wait timed out while tuning");
@@ -783,25 +890,28 @@ int time_group(mdsx_batch* b, const BatchGroup& g, int reps, double* us) {
 
 extern "C" {
 
-// Test and tuning hook: fixes the shape (rows per warp, CTAs per SM) of the
-// group of embedding dimension p; rows_per_warp 0 removes the override.
-int mdsx_batch_force_shape(mdsx_batch* b, int p, int rows_per_warp, int ctas_per_sm) {
+// Test and tuning hook: fixes the shape of the group of embedding dimension p:
+// schedule (0 stream-K, 1 row-block queue), rows per warp, CTAs per SM;
+// rows_per_warp 0 removes the override.
+int mdsx_batch_force_shape(mdsx_batch* b, int p, int schedule, int rows_per_warp, int ctas_per_sm) {
     if (!b) return MDSX_EINVAL;
     const std::pair<int, int> key{p, b->trunc ? 1 : 0};
     if (rows_per_warp == 0) {
         b->forced.erase(key);
     } else {
-        if (!mdsx::batch::rw_built(p, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4)
-            return bfail(b, MDSX_EINVAL, "rows per warp not built for this dimension, or CTAs per SM outside 1..4");
-        b->forced[key] = {rows_per_warp, ctas_per_sm};
+        if (!mdsx::batch::rw_built(p, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4 ||
+            (schedule != 0 && schedule != 1))
+            return bfail(b, MDSX_EINVAL,
+                         "schedule not 0 or 1, rows per warp not built for this dimension, or CTAs per SM outside 1..4");
+        b->forced[key] = Shape{schedule, rows_per_warp, ctas_per_sm};
     }
     free_plan(b);
     b->results_known = false;
     return MDSX_OK;
 }
 
-// Autotuner: times every built (rows per warp, CTAs per SM) candidate of each
-// group on this batch (`repetitions` launches each, after two warm-ups) and
+// Autotuner: times every built (schedule, rows per warp, CTAs per SM)
+// candidate of each group on this batch (`repetitions` launches each, after two warm-ups) and
 // caches the fastest per (P, N-bucket, truncation); later plans of any batch
 // in this process (and in others, through MDSX_TUNE_CACHE) use it. Writes the
 // number of candidates timed to *candidates when non-NULL.
@@ -821,45 +931,46 @@ int mdsx_batch_tune(mdsx_batch* b, int repetitions, int* candidates) {
         keys.push_back({g.p, g.trunc ? 1 : 0, mdsx::batch::n_bucket(mean_n / g.members.size())});
     }
     int timed = 0;
-    std::map<std::pair<int, int>, std::pair<int, int>> best_shape;
+    std::map<std::pair<int, int>, Shape> best_shape;
     std::map<std::pair<int, int>, double> best_us;
-    for (int rw : {1, 2, 4})
-        for (int ctas : {1, 2}) {
-            std::map<std::pair<int, int>, std::pair<int, int>> force;
-            bool any = false;
-            for (const auto& k : keys)
-                if (mdsx::batch::rw_built(k.p, rw)) {
-                    int occ = 0;
-                    size_t local = 0;
-                    if (mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local) != cudaSuccess || occ < ctas)
-                        continue;
-                    force[{k.p, k.trunc}] = {rw, ctas};
-                    any = true;
-                }
-            if (!any) continue;
-            if ((rc = plan(b, &force))) return rc;
-            if ((rc = upload_descriptors(b))) return rc;
-            for (const auto& g : b->groups) {
-                const std::pair<int, int> key{g.p, g.trunc ? 1 : 0};
-                auto f = force.find(key);
-                if (f == force.end() || g.rw != rw || g.ctas_per_sm != ctas) continue;
-                double us = 0.0;
-                if ((rc = time_group(b, g, repetitions, &us))) return rc;
-                ++timed;
-                if (!best_us.count(key) || us < best_us[key]) {
-                    best_us[key] = us;
-                    best_shape[key] = {rw, ctas};
+    for (int sched : {0, 1})
+        for (int rw : {1, 2, 4})
+            for (int ctas : {1, 2}) {
+                std::map<std::pair<int, int>, Shape> force;
+                bool any = false;
+                for (const auto& k : keys)
+                    if (mdsx::batch::rw_built(k.p, rw)) {
+                        int occ = 0;
+                        size_t local = 0;
+                        const cudaError_t ce = sched == 0 ? mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local)
+                                                          : mdsx::batch::occupancy_queue(k.p, k.trunc != 0, rw, &occ);
+                        if (ce != cudaSuccess || occ < ctas) continue;
+                        force[{k.p, k.trunc}] = Shape{sched, rw, ctas};
+                        any = true;
+                    }
+                if (!any) continue;
+                if ((rc = plan(b, &force))) return rc;
+                if ((rc = upload_descriptors(b))) return rc;
+                for (const auto& g : b->groups) {
+                    const std::pair<int, int> key{g.p, g.trunc ? 1 : 0};
+                    if (!force.count(key) || g.schedule != sched || g.rw != rw || g.ctas_per_sm != ctas) continue;
+                    double us = 0.0;
+                    if ((rc = time_group(b, g, repetitions, &us))) return rc;
+                    ++timed;
+                    if (!best_us.count(key) || us < best_us[key]) {
+                        best_us[key] = us;
+                        best_shape[key] = Shape{sched, rw, ctas};
+                    }
                 }
             }
-        }
     {
         std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
         mdsx::batch::load_cache_locked();
         for (const auto& k : keys) {
             const std::pair<int, int> key{k.p, k.trunc};
             if (!best_shape.count(key)) continue;
-            mdsx::batch::g_tune[{k.p, k.bucket, k.trunc}] = {best_shape[key].first, best_shape[key].second,
-                                                               best_us[key]};
+            const Shape& w = best_shape[key];
+            mdsx::batch::g_tune[{k.p, k.bucket, k.trunc}] = {w.schedule, w.rw, w.ctas, best_us[key]};
         }
         mdsx::batch::save_cache_locked();
     }

@@ -2,6 +2,7 @@
 // batch_sweep_lo.cu and batch_sweep_hi.cu).
 #pragma once
 
+#include "batch_queue.cuh"
 #include "batch_sweep.h"
 
 namespace mdsx {
@@ -29,6 +30,34 @@ cudaError_t occupancy_one(int* ctas, size_t* local_bytes) {
     if (e != cudaSuccess) return e;
     *local_bytes = attr.localSizeBytes;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, batch_sweep_kernel<P, TRUNC, RW>, kThreads, smem);
+}
+
+template <int P, bool TRUNC, int RW>
+cudaError_t launch_queue_one(const QueueArgs& a, int grid, cudaStream_t st) {
+    constexpr int smem = QueueShape<P, RW>::kSmemBytes;
+    cudaError_t e =
+        cudaFuncSetAttribute(batch_queue_kernel<P, TRUNC, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    batch_queue_kernel<P, TRUNC, RW><<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int P, bool TRUNC, int RW>
+cudaError_t occupancy_queue_one(int* ctas) {
+    constexpr int smem = QueueShape<P, RW>::kSmemBytes;
+    cudaError_t e =
+        cudaFuncSetAttribute(batch_queue_kernel<P, TRUNC, RW>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, batch_queue_kernel<P, TRUNC, RW>, kThreads, smem);
+}
+
+template <int P, int RW>
+cudaError_t launch_queue_p(bool trunc, const QueueArgs& a, int grid, cudaStream_t st) {
+    return trunc ? launch_queue_one<P, true, RW>(a, grid, st) : launch_queue_one<P, false, RW>(a, grid, st);
+}
+template <int P, int RW>
+cudaError_t occupancy_queue_p(bool trunc, int* ctas) {
+    return trunc ? occupancy_queue_one<P, true, RW>(ctas) : occupancy_queue_one<P, false, RW>(ctas);
 }
 
 template <int P, int RW>

@@ -7,6 +7,7 @@
 #include <cstddef>
 
 #include "batch_kernel.cuh"
+#include "batch_queue.cuh"
 
 namespace mdsx {
 namespace batch {
@@ -19,9 +20,15 @@ int smem_bytes(int p, int rw);
 cudaError_t occupancy(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes);
 cudaError_t launch(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st);
 
+// Row-block queue schedule (batch_queue.cuh).
+cudaError_t occupancy_queue(int p, bool trunc, int rw, int* ctas_per_sm);
+cudaError_t launch_queue(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st);
+
 #define MDSX_BATCH_DECLARE(R)                                                                  \
     cudaError_t occupancy_##R(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes); \
-    cudaError_t launch_##R(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st);
+    cudaError_t launch_##R(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t st);      \
+    cudaError_t occupancy_queue_##R(int p, bool trunc, int rw, int* ctas_per_sm);                 \
+    cudaError_t launch_queue_##R(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st);
 MDSX_BATCH_DECLARE(lo)
 MDSX_BATCH_DECLARE(hi)
 #undef MDSX_BATCH_DECLARE

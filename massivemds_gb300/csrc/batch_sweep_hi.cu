@@ -36,5 +36,37 @@ cudaError_t occupancy_hi(int p, bool trunc, int rw, int* ctas_per_sm, size_t* lo
 #undef ARGS
 }
 
+cudaError_t launch_queue_hi(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st) {
+#define FN launch_queue_p
+#define ARGS trunc, a, grid, st
+    switch (p) {
+        MDSX_BATCH_CASE(5)
+        MDSX_BATCH_CASE(6)
+        MDSX_BATCH_CASE(7)
+        MDSX_BATCH_CASE(8)
+        MDSX_BATCH_CASE(9)
+        MDSX_BATCH_CASE(10)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
+cudaError_t occupancy_queue_hi(int p, bool trunc, int rw, int* ctas_per_sm) {
+#define FN occupancy_queue_p
+#define ARGS trunc, ctas_per_sm
+    switch (p) {
+        MDSX_BATCH_CASE(5)
+        MDSX_BATCH_CASE(6)
+        MDSX_BATCH_CASE(7)
+        MDSX_BATCH_CASE(8)
+        MDSX_BATCH_CASE(9)
+        MDSX_BATCH_CASE(10)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
 }  // namespace batch
 }  // namespace mdsx

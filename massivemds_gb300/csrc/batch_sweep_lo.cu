@@ -32,5 +32,33 @@ cudaError_t occupancy_lo(int p, bool trunc, int rw, int* ctas_per_sm, size_t* lo
 #undef ARGS
 }
 
+cudaError_t launch_queue_lo(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st) {
+#define FN launch_queue_p
+#define ARGS trunc, a, grid, st
+    switch (p) {
+        MDSX_BATCH_CASE(1)
+        MDSX_BATCH_CASE(2)
+        MDSX_BATCH_CASE(3)
+        MDSX_BATCH_CASE(4)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
+cudaError_t occupancy_queue_lo(int p, bool trunc, int rw, int* ctas_per_sm) {
+#define FN occupancy_queue_p
+#define ARGS trunc, ctas_per_sm
+    switch (p) {
+        MDSX_BATCH_CASE(1)
+        MDSX_BATCH_CASE(2)
+        MDSX_BATCH_CASE(3)
+        MDSX_BATCH_CASE(4)
+        default: return cudaErrorInvalidValue;
+    }
+#undef FN
+#undef ARGS
+}
+
 }  // namespace batch
 }  // namespace mdsx

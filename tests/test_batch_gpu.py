@@ -2,7 +2,7 @@
 batch_kernel.cuh) against the oracle, instance by instance: every instance's
 sum of increments and gradient within 1e-5 relative of the FP64 oracle on its
 FP32-rounded delta (the FP32 bar of the single-instance engine), for uneven N,
-mixed P, every built tile shape, missing pairs, single-location updates and
+mixed P, both schedules and every built tile shape, missing pairs, single-location updates and
 precision changes; plus determinism and the autotuner."""
 import numpy as np
 import pytest
@@ -65,15 +65,42 @@ def test_mixed_instances_match_oracle():
         assert _rel(ll, oracle.log_likelihood(oracle.sum_of_increments(delta, x, tau), x.shape[0], tau)) < TOL
 
 
-@pytest.mark.parametrize("p,rw,ctas", [(2, 1, 2), (2, 2, 1), (2, 4, 2), (3, 1, 1), (3, 2, 2), (3, 4, 1),
-                                       (6, 1, 2), (6, 2, 1)])
-def test_every_shape_matches_oracle(p, rw, ctas):
+SHAPES = [(2, 1, 2), (2, 2, 1), (2, 4, 2), (3, 1, 1), (3, 2, 2), (3, 4, 1), (6, 1, 2), (6, 2, 1)]
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+@pytest.mark.parametrize("p,rw,ctas", SHAPES)
+def test_every_shape_matches_oracle(schedule, p, rw, ctas):
     problems = _problems([(257, p), (640, p), (129, p), (1000, p)], 10 + rw)
     with Batch() as b:
         _fill(b, problems)
-        b.force_shape(p, rw, ctas)
-        assert b.group_shape(p)[:2] == (rw, ctas)
+        b.force_shape(p, rw, ctas, schedule)
+        assert b.group_shape(p)[:3] == (schedule, rw, ctas)
         _check(b, problems)
+
+
+def test_schedules_agree_and_gradients_concatenate_in_instance_order():
+    torch = pytest.importorskip("torch")
+    problems = _problems([(300, 6), (700, 2), (451, 3), (1200, 2)], 12)
+    grads = {}
+    for schedule in (0, 1):
+        with Batch() as b:
+            _fill(b, problems)
+            for p in (2, 3, 6):
+                b.force_shape(p, 1, 2, schedule)
+            total = sum(x.size for _, x, _ in problems)
+            d_sums = torch.zeros(4 * len(problems), dtype=torch.float64, device="cuda")
+            d_grads = torch.zeros(total, dtype=torch.float64, device="cuda")
+            b.evaluate_device(d_sums.data_ptr(), d_grads.data_ptr())
+            torch.cuda.synchronize()
+            g = d_grads.cpu().numpy()
+            off = 0
+            for k, (_, x, _) in enumerate(problems):
+                assert np.array_equal(g[off:off + x.size], b.getLogLikelihoodGradient(k))
+                off += x.size
+            grads[schedule] = g
+    # same tile shape, two schedules: the row partials are summed in different orders
+    assert np.abs(grads[0] - grads[1]).max() <= 1e-5 * np.abs(grads[1]).max()
 
 
 def test_without_truncation():
@@ -142,6 +169,6 @@ def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
         _fill(b, problems)
         assert b.tune(repetitions=3) >= 3
         for p in (2, 3, 6):
-            rw, ctas, grid = b.group_shape(p)
-            assert rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
+            sc, rw, ctas, grid = b.group_shape(p)
+            assert sc in (0, 1) and rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
         _check(b, problems)
