@@ -136,14 +136,20 @@ __global__ void __launch_bounds__(kThreads, MDSX_F32_MIN_CTAS) batch_queue_kerne
                 }
             }
             // end marker: a stage that completes without data
+            bool ended = false;
             if (ok && mbar_wait_bounded(&empty[stage], phase ^ 1u, a.err, kDevTimeoutEmpty)) {
                 meta[stage] = make_int4(-1, 0, 0, 0);
                 mbar_arrive(&full[stage]);
+                ended = true;
             }
-            // let this thread's copies land before the CTA can exit
+            // Let this thread's copies land before the CTA can exit: the last
+            // stages issued, walking back from the end-marker slot. That slot's
+            // earlier data stage was released by every consumer before the
+            // marker went in (and its barrier has moved on), so it is skipped.
             int s = stage;
             uint32_t ph = phase;
-            const int pending = issued < kStages ? (int)issued : kStages;
+            const int window = ended ? kStages - 1 : kStages;
+            const int pending = issued < window ? (int)issued : window;
             for (int j = 0; j < pending; ++j) {
                 if (--s < 0) {
                     s = kStages - 1;
