@@ -54,7 +54,8 @@ constexpr int kStepCols = 128;                       // columns per stage: 32 la
 #define MDSX_F32_MIN_CTAS 2
 #endif
 constexpr int kStages = MDSX_STAGES;  // depth of the TMA ring
-constexpr int kLogFoldPairs = 64;                    // product of <= 64 factors in [1, 2] cannot overflow
+constexpr int kLogFoldPairs = 64;
+constexpr int kLogFoldF64Stages = 64;  // FP64: 256 factors >= 1/2 per product stay above 1e-78                    // product of <= 64 factors in [1, 2] cannot overflow
 
 struct SweepArgs {
     int n;               // locations N
@@ -210,11 +211,13 @@ __device__ __forceinline__ void pair2_f32(const f2 (&xi)[P], const f2 (&xj)[P], 
     for (int q = 0; q < P; ++q) g[q] = ffma2(c, dx[q], g[q]);
 }
 
-// One ordered pair in FP64 (CUDA double sqrt/erfc/exp/log).
+// One ordered pair in FP64 (CUDA double sqrt/erfc/exp). log Phi is not taken
+// per pair: Phi multiplies into lprod (Phi >= 1/2 for d >= 0) and the caller
+// folds log(lprod) into the row's sum every kLogFoldF64Stages stages.
 template <int P, bool TRUNC, bool MASKED>
 __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&xj)[P][4], int c, double delta,
                                          bool valid, double tau, double sqrt_tau, double (&g)[P], double& r2,
-                                         double& lsum) {
+                                         double& lprod) {
     double dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = xi[q] - xj[q][c];
@@ -225,14 +228,18 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
     const double d = sqrt(d2);
     double res = delta - d;
     r2 = fma(res, res, r2);
+    double cc;
     if (TRUNC) {
         const double z = d * sqrt_tau;
         const double cdf = 0.5 * erfc(-z * 0.70710678118654752440);
-        lsum += log(cdf);
+        lprod *= cdf;
         const double pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
-        res -= pdf / (cdf * sqrt_tau);
+        // (res - pdf / (cdf sqrt_tau)) / d with one division
+        const double den = cdf * sqrt_tau;
+        cc = fma(res, den, -pdf) / (den * d);
+    } else {
+        cc = res / d;
     }
-    const double cc = res / d;
 #pragma unroll
     for (int q = 0; q < P; ++q) g[q] = fma(cc, dx[q], g[q]);
 }
@@ -281,7 +288,7 @@ template <int P, bool TRUNC, bool MASKED, int RW, typename S>
 __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const double* __restrict__ xtile,
                                           const double (&xi)[RW][P], int i0, int j0, int n, int lane, double tau,
                                           double sqrt_tau, double (&g)[RW][P], double (&r2)[RW],
-                                          double (&lsum)[RW]) {
+                                          double (&lprod)[RW]) {
     double xj[P][4];
 #pragma unroll
     for (int q = 0; q < P; ++q) {
@@ -307,7 +314,7 @@ __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const dou
                 const int i = i0 + r, j = j0 + 4 * lane + c;
                 valid = (j < n) && (i < n) && (i != j) && (dl[c] == dl[c]);
             }
-            pair_f64<P, TRUNC, MASKED>(xi[r], xj, c, dl[c], valid, tau, sqrt_tau, g[r], r2[r], lsum[r]);
+            pair_f64<P, TRUNC, MASKED>(xi[r], xj, c, dl[c], valid, tau, sqrt_tau, g[r], r2[r], lprod[r]);
         }
     }
 }
@@ -456,9 +463,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
             }
         }
 
-        // FP64 accumulators: gradient, r^2 and logPhi sums per row.
+        // FP64 accumulators: gradient, r^2 and logPhi sums per row, and the
+        // running product of Phi between log folds.
         C g[RW][P];
-        C r2[RW], acc2[RW];
+        C r2[RW], acc2[RW], prod64[RW];
         // FP32 accumulators (packs): negated gradient, r^2 per fold interval,
         // running product of 1/Phi; and the compensated segment sums.
         f2 g2[RW][P], r2p = pk(0.f, 0.f), prodp = pk(1.f, 1.f);
@@ -466,6 +474,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
         for (int r = 0; r < RW; ++r) {
             r2[r] = C(0);
             acc2[r] = C(0);
+            prod64[r] = C(1);
 #pragma unroll
             for (int q = 0; q < P; ++q) {
                 g[r][q] = C(0);
@@ -492,10 +501,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
             } else {
                 if (masked)
                     stage_f64<P, TRUNC, true, RW>(dtile, xtile, xi, row0, j0, a.n, lane, a.tau, a.sqrt_tau, g, r2,
-                                                  acc2);
+                                                  prod64);
                 else
                     stage_f64<P, TRUNC, false, RW>(dtile, xtile, xi, row0, j0, a.n, lane, a.tau, a.sqrt_tau, g,
-                                                   r2, acc2);
+                                                   r2, prod64);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[stage]);
@@ -519,6 +528,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                     two_sum(r2_hi, step_sum, hi, e);
                     r2_hi = hi;
                     r2_lo += e;
+                }
+            } else if (TRUNC) {
+                // 4 factors per row and stage, each in [1/2, 1]: fold well before underflow
+                if ((s + 1) % kLogFoldF64Stages == 0 || s + 1 == steps) {
+#pragma unroll
+                    for (int r = 0; r < RW; ++r) {
+                        acc2[r] += log(prod64[r]);
+                        prod64[r] = C(1);
+                    }
                 }
             }
         }
