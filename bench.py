@@ -172,6 +172,23 @@ def make_delta(n):
     return gen.noisy_delta(n, dim=10, noise_sd=0.05, seed=666, dtype=np.float32)
 
 
+def across_ranks_max(value: float, world: int, device) -> float:
+    """The largest value over all ranks (every rank gets it); the job's time is
+    its slowest replica's."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -266,12 +283,8 @@ def run_mdsx(args):
     launches = eng.last_launch_count()  # sweep launches per evaluation
     gpu_launches = args.steps * EVALS_PER_STEP * (launches + 1)  # + the location conversion kernel
 
-    if world > 1:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    total_evals = args.steps * EVALS_PER_STEP * world
-    value = total_evals / (elapsed_ms / 1000.0)
+    elapsed_ms = across_ranks_max(elapsed_ms, world, f"cuda:{local}")
+    value = job_throughput(args.steps * EVALS_PER_STEP, world, elapsed_ms / 1000.0)
 
     # end to end through the reference-facing API with host buffers
     eng.set_stream(None)
@@ -292,11 +305,8 @@ def run_mdsx(args):
             eng.getSumOfIncrements()
             eng.getLogLikelihoodGradient(g_np)
     e2e_s = time.perf_counter() - t
-    if world > 1:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e_value = e2e_steps * EVALS_PER_STEP * world / e2e_s
+    e2e_s = across_ranks_max(e2e_s, world, f"cuda:{local}")
+    e2e_value = job_throughput(e2e_steps * EVALS_PER_STEP, world, e2e_s)
 
     hbm_peak, peak_kind = peaks()
     bytes_per_launch = float(n) * n * 4 + 2.0 * n * P * 4
