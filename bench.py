@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--impl", default="mdsx", choices=["mdsx", "reference"])
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--cpu-seconds", type=float, default=4.0, help="wall time of one CPU baseline sample")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "c1"],
+                    help="sweep: the headline N=20000 FP32 sweep; c1: the reference's benchmark case "
+                         "(N=1000, FP64, 100 iterations through the host API)")
     return ap.parse_args()
 
 
@@ -187,6 +190,78 @@ def across_ranks_max(value: float, world: int, device) -> float:
 def job_throughput(units_per_rank: int, world: int, seconds: float) -> float:
     """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
     return units_per_rank * world / seconds
+
+
+def run_c1(args):
+    """The reference's own benchmark case: N = 1000, P = 2, FP64, truncation,
+    tau = 1, delta = distances of 1000 points iid N(0, I_10), x ~ N(0, 1); one
+    iteration = updateLocations(-1, x) + getLogLikelihood() +
+    getLogLikelihoodGradient() through the engine's host API (the call sequence
+    src/benchmark.cpp:250-309 times on its CPU engines). cpu_baseline: the same
+    per-iteration work in the oracle's C port of the reference serial engine,
+    on all host threads."""
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import massivemds_gb300 as m
+    from massivemds_gb300 import data as gen
+
+    n, p, tau, iters = 1000, 2, 1.0, 100
+    delta = gen.euclidean_delta(n, dim=10, seed=666)
+    xs = np.random.default_rng(667).standard_normal((args.warmup + args.steps, iters, n, p))
+    e = m.Engine(p, n, m.flags.LEFT_TRUNCATION, local)
+    e.setPairwiseData(delta)
+    e.setParameters([tau])
+    grad = np.empty(n * p)
+
+    def step(batch):
+        for k in range(iters):
+            e.updateLocations(-1, batch[k])
+            e.getLogLikelihood()
+            e.getLogLikelihoodGradient(grad)
+
+    for w in range(args.warmup):
+        step(xs[w])
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for s_ in range(args.steps):
+        step(xs[args.warmup + s_])
+    t1 = time.time()
+    sampler.stop()
+    e.close()
+    sec_per_step = (t1 - t0) / args.steps
+    value = iters / sec_per_step
+
+    import oracle  # cpu_baseline leg
+
+    cores = os.cpu_count() or 1
+    t = time.perf_counter()
+    sample_iters = 10
+    for k in range(sample_iters):
+        oracle.sum_of_increments(delta, xs[0, k], tau, True, threads=cores)
+        oracle.gradient(delta, xs[0, k], tau, True, threads=cores)
+    cpu_value = sample_iters / (time.perf_counter() - t)
+    line = {
+        "metric": "iterations/s (updateLocations + getLogLikelihood + getLogLikelihoodGradient)",
+        "value": value, "unit": "iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * sec_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic: delta = ||Y_i - Y_j||, Y ~ N(0, I_10) (seed 666); x ~ N(0,1) per iteration",
+        "config": {"workload": "reference benchmark case: N=1000, P=2, FP64, truncation, tau=1, 100 iterations "
+                               "per step through the host API", "n": n, "p": p, "tau": tau,
+                   "iterations_per_step": iters, "l2": "delta 8 MB stays in L2 (timed as a user would see it)"},
+        "e2e": {"value": value, "unit": "iterations/s", "h2d_bytes_per_step": iters * n * p * 8,
+                "d2h_bytes_per_step": iters * (n * p * 8 + 8)},
+        "clocks": sampler.summary(t0, t1),
+        "cpu_baseline": {"value": cpu_value, "unit": "iterations/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample_iters} iterations of the same workload"},
+    }
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(args):
@@ -344,7 +419,12 @@ def run_mdsx(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "c1":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the c1 workload's CPU time is its cpu_baseline"}))
+        else:
+            run_c1(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_mdsx(args)
