@@ -12,8 +12,10 @@ arithmetic with compensated FP32 partials and FP64 reductions.
   e2e    the same evaluations through the reference-facing API with host
          buffers: updateLocations(-1, x) / getSumOfIncrements() /
          getLogLikelihoodGradient(out), copies inside the timed region.
-  roofline  the sweep kernel's algorithmic bytes per launch (N^2 * 4 + 2 N P * 4)
-         over its mean CUDA-event duration, against the measured HBM peak.
+  roofline  the sweep's algorithmic bytes per evaluation (N^2 * 4 + 2 N P * 4)
+         over the mean CUDA-event duration of its kernels (the unordered-pair
+         sweep and its finish kernel, or the row-block sweep with --schedule
+         rows), against the measured HBM peak.
   cpu_baseline  the oracle's port of the reference's per-evaluation work
          (likelihood pass + gradient pass, libm transcendentals) on all host
          cores over a bounded sample of rows, scaled to evals/s.
@@ -55,6 +57,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mdsx", choices=["mdsx", "reference"])
     ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--schedule", default="pairs", choices=["pairs", "rows"],
+                    help="sweep schedule: each unordered pair once (default) or the row-block schedule")
     ap.add_argument("--cpu-seconds", type=float, default=4.0, help="wall time of one CPU baseline sample")
     ap.add_argument("--workload", default="sweep", choices=["sweep", "c1"],
                     help="sweep: the headline N=20000 FP32 sweep; c1: the reference's benchmark case "
@@ -79,9 +83,10 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per sweep launch from the committed ncu summary, if present."""
-    path = os.path.join(REPO, "profiles", "sweep_f32_n20000.txt")
+def profiled_traffic(schedule):
+    """DRAM bytes per evaluation from the committed ncu summary of that schedule, if present."""
+    name = "pair_sweep_f32_n20000.txt" if schedule == "pairs" else "sweep_f32_n20000.txt"
+    path = os.path.join(REPO, "profiles", name)
     try:
         with open(path) as f:
             for line in f:
@@ -309,6 +314,7 @@ def run_mdsx(args):
     n = args.n
     delta = make_delta(n)
     eng = m.Engine(P, n, m.flags.FLOAT | m.flags.LEFT_TRUNCATION, local)
+    eng.set_sweep_schedule(m.flags.SWEEP_PAIRS if args.schedule == "pairs" else m.flags.SWEEP_ROWS)
     eng.setPairwiseData(delta)
     eng.setParameters([TAU])
     stream = torch.cuda.Stream()
@@ -386,7 +392,9 @@ def run_mdsx(args):
     hbm_peak, peak_kind = peaks()
     bytes_per_launch = float(n) * n * 4 + 2.0 * n * P * 4
     achieved = bytes_per_launch / (kernel_ms / 1000.0) / 1e9
-    traffic = profiled_traffic() if n == N else None  # the committed capture is of N = 20000
+    traffic = profiled_traffic(args.schedule) if n == N else None  # the committed captures are of N = 20000
+    kernel_name = ("pair_kernel<2,true> + pair_finish_kernel<2>" if args.schedule == "pairs"
+                   else "sweep_kernel<float,float,2,true>")
 
     line = None
     if rank == 0:
@@ -397,11 +405,12 @@ def run_mdsx(args):
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
             "config": {"workload": workload(n), "n": n, "p": P, "tau": TAU, "evals_per_step": EVALS_PER_STEP,
+                       "schedule": args.schedule,
                        "delta_bytes": n * n * 4, "l2": f"inputs larger than L2 ({n * n * 4 / 1e9:.2f} GB delta vs 129 MB L2), no flush",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": "sweep_kernel<float,float,2,true>", "kernel_ms": kernel_ms,
+                         "kernel": kernel_name, "kernel_ms": kernel_ms,
                          "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": EVALS_PER_STEP * n * P * 8,

@@ -135,6 +135,19 @@ int mdsx_evaluate_device(mdsx_engine* engine, double* d_sum, double* d_gradient)
 /* Number of kernel launches the last sweep issued (for launch accounting). */
 int mdsx_last_launch_count(mdsx_engine* engine, int* out);
 
+/* Sweep schedule (no counterpart in the reference; results agree within the
+ * FP32 tolerance, the summation order differs):
+ *   MDSX_SWEEP_ROWS  - one pass per ordered pair, row blocks x 128-column stages;
+ *   MDSX_SWEEP_PAIRS - each unordered pair {i, j} once: distance and Phi shared
+ *                      by (i, j) and (j, i), each direction with its own delta;
+ *                      a sweep kernel plus a finish kernel. FP32 mode, P <= 4.
+ * New engines use MDSX_SWEEP_PAIRS where it is built, else MDSX_SWEEP_ROWS.
+ * Setting MDSX_SWEEP_PAIRS where it is not built returns MDSX_EUNSUPPORTED. */
+#define MDSX_SWEEP_ROWS 0
+#define MDSX_SWEEP_PAIRS 1
+int mdsx_set_sweep_schedule(mdsx_engine* engine, int schedule);
+int mdsx_get_sweep_schedule(mdsx_engine* engine, int* out);
+
 /* ---- Learned gradient surrogate (no counterpart in the reference) ----
  * g_i ~= s * sum_k alpha_ik (x_i - x_{l_k}) over K landmark locations (a
  * seeded random subset), alpha_i = MLP(features_i) with rotation-invariant

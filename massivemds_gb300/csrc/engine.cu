@@ -27,6 +27,7 @@
 
 #include "../../include/mdsx.h"
 #include "normal_rational.h"
+#include "pair_kernel.cuh"
 #include "engine_internal.h"
 #include "sweep.h"
 
@@ -66,7 +67,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
 long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
 int make_tmap_2d(mdsx_engine* e, CUtensorMap* map, void* base, bool f32, long long cols, long long rows,
-                 long long ld_elems, unsigned box_cols, unsigned box_rows) {
+                 long long ld_elems, unsigned box_cols, unsigned box_rows,
+                 CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE) {
     auto fn = encode_tiled();
     if (!fn) return fail(e, MDSX_ECUDA, "cuTensorMapEncodeTiled unavailable from the driver");
     const int elem = f32 ? 4 : 8;
@@ -75,7 +77,7 @@ int make_tmap_2d(mdsx_engine* e, CUtensorMap* map, void* base, bool f32, long lo
     cuuint32_t box[2] = {box_cols, box_rows};
     cuuint32_t estride[2] = {1, 1};
     CUresult r = fn(map, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, base, gdim,
-                    gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         char buf[128];
@@ -98,8 +100,50 @@ void free_all(mdsx_engine* e) {
     cudaFree(e->d_lrow);
     cudaFree(e->d_counts);
     cudaFree(e->d_row_nan);
+    cudaFree(e->d_rowpart);
+    cudaFree(e->d_colpart);
+    cudaFree(e->d_plpart);
     if (e->h_out) cudaFreeHost(e->h_out);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
+}
+
+// Unordered-pair schedule: units (J, I), I >= 4J, split evenly over
+// G <= U CTAs; scratch for row, column and likelihood partials; tensor maps of
+// delta (plain and 128-byte swizzled boxes) and of both location buffers.
+int plan_pairs(mdsx_engine* e) {
+    int ctas = 0;
+    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, &ctas));
+    if (ctas < 1) return fail(e, MDSX_ECUDA, "pair sweep kernel cannot be resident on this device");
+    e->pair_nb = (e->n + mdsx::kPairCols - 1) / mdsx::kPairCols;
+    e->pair_nc = (e->n + mdsx::kPairRows - 1) / mdsx::kPairRows;
+    e->pair_units = mdsx::pair_units_before(e->pair_nb, e->pair_nc);
+    e->pair_grid = (int)std::min<long long>(e->pair_units, (long long)e->sm_count * ctas);
+    e->pair_max_slots = 1;
+    for (int J = 0; J < e->pair_nb; ++J) {
+        const long long u0 = mdsx::pair_units_before(J, e->pair_nc);
+        const long long u1 = u0 + (e->pair_nc - 4 * J) - 1;
+        const int slots = mdsx::cta_of_unit(u1, e->pair_units, e->pair_grid) -
+                          mdsx::cta_of_unit(u0, e->pair_units, e->pair_grid) + 1;
+        e->pair_max_slots = std::max(e->pair_max_slots, slots);
+    }
+    MDSX_CUDA(e, cudaMalloc(&e->d_rowpart, (size_t)e->pair_units * mdsx::kPairRows * e->p * sizeof(float)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_colpart, (size_t)e->pair_nb * e->pair_max_slots * mdsx::kPairWarps * e->p *
+                                               mdsx::kPairCols * sizeof(float)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_plpart, (size_t)e->pair_grid * mdsx::kPairWarps * 2 * sizeof(double)));
+    for (int b = 0; b < 2; ++b) {
+        mdsx::PairMaps& m = e->pair_maps[b];
+        int rc = make_tmap_2d(e, &m.a, e->d_delta, true, e->n, e->n, e->ld, mdsx::kPairCols, mdsx::kPairRows);
+        if (!rc)
+            rc = make_tmap_2d(e, &m.b, e->d_delta, true, e->n, e->n, e->ld, mdsx::kPairRows, mdsx::kPairCols,
+                              CU_TENSOR_MAP_SWIZZLE_128B);
+        // the location maps span x_ld columns, so the flags of rows >= N are read from memory (1), not filled
+        if (!rc)
+            rc = make_tmap_2d(e, &m.xi, e->d_x[b], true, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairRows, e->p + 1);
+        if (!rc)
+            rc = make_tmap_2d(e, &m.xj, e->d_x[b], true, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairCols, e->p + 1);
+        if (rc) return rc;
+    }
+    return MDSX_OK;
 }
 
 int plan_and_allocate(mdsx_engine* e) {
@@ -127,7 +171,8 @@ int plan_and_allocate(mdsx_engine* e) {
     const int delta_elem = e->shape.delta_elem_bytes;
     e->ld = round_up(e->n, 16 / delta_elem);
     e->x_ld = (int)std::max<long long>(round_up(e->n, mdsx::kStepCols), e->rows_padded);
-    const size_t x_bytes = (size_t)e->p * e->x_ld * e->shape.x_elem_bytes;
+    // P location rows and one flag row (read by the unordered-pair schedule)
+    const size_t x_bytes = (size_t)(e->p + 1) * e->x_ld * e->shape.x_elem_bytes;
     const size_t acc_bytes = e->x_f32 ? 4 : 8;
 
     MDSX_CUDA(e, cudaMalloc(&e->d_delta, (size_t)e->n * e->ld * delta_elem));
@@ -156,8 +201,25 @@ int plan_and_allocate(mdsx_engine* e) {
         rc = make_tmap_2d(e, &e->tmap_x[b], e->d_x[b], e->x_f32, e->n, e->p, e->x_ld, mdsx::kStepCols, e->p);
         if (rc) return rc;
     }
+    if (mdsx::pair_built(e->mode, e->p)) {
+        rc = plan_pairs(e);
+        if (rc) return rc;
+        e->schedule = MDSX_SWEEP_PAIRS;
+    }
     MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
     return MDSX_OK;
+}
+
+// Flag row (row P) of both FP32 location buffers from the NaN-row marks.
+cudaError_t write_flags(mdsx_engine* e) {
+    if (!e->x_f32) return cudaSuccess;
+    for (int b = 0; b < 2; ++b) {
+        cudaError_t err = mdsx::write_flag_row(e->d_row_nan, e->n, e->rows_padded,
+                                               static_cast<float*>(e->d_x[b]) + (size_t)e->p * e->x_ld, e->x_ld,
+                                               e->stream);
+        if (err != cudaSuccess) return err;
+    }
+    return cudaSuccess;
 }
 
 // Clears the error word and self-resetting counters after a failed sweep.
@@ -210,6 +272,34 @@ int enqueue_sweep(mdsx_engine* e) {
     if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
     if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
     SweepArgs a = make_args(e);
+    if (e->schedule == MDSX_SWEEP_PAIRS) {
+        mdsx::PairArgs pa{};
+        pa.n = e->n;
+        pa.nb = e->pair_nb;
+        pa.nc = e->pair_nc;
+        pa.grid = e->pair_grid;
+        pa.max_slots = e->pair_max_slots;
+        pa.truncation = a.truncation;
+        pa.n_units = e->pair_units;
+        pa.k_e = a.k_e;
+        pa.log2_k2 = a.log2_k2;
+        pa.tp0 = a.tp0;
+        pa.tp1 = a.tp1;
+        pa.tp2 = a.tp2;
+        pa.ts0 = a.ts0;
+        pa.ts1 = a.ts1;
+        pa.ts2 = a.ts2;
+        pa.tau = a.tau;
+        pa.rowpart = e->d_rowpart;
+        pa.colpart = e->d_colpart;
+        pa.lpart = e->d_plpart;
+        pa.grad_out = a.grad_out;
+        pa.sums_out = a.sums_out;
+        pa.err = a.err;
+        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->pair_maps[e->xcur], pa, e->stream));
+        e->last_launches = 2;
+        return MDSX_OK;
+    }
     MDSX_CUDA(e, mdsx::sweep_launch(e->mode, e->p, e->trunc, e->grid, e->tmap_delta, e->tmap_x[e->xcur], a,
                                     e->stream));
     e->last_launches = 1;
@@ -428,6 +518,7 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
         cudaFree(staging);
     }
     MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, e->delta_f32, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+    MDSX_CUDA(e, write_flags(e));
     MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
     e->data_set = true;
     e->sum_known = e->grad_known = false;
@@ -443,6 +534,7 @@ int mdsx_set_pairwise_data_f32(mdsx_engine* e, const float* data, size_t length)
         MDSX_CUDA(e, cudaMemcpy2DAsync(e->d_delta, (size_t)e->ld * sizeof(float), data, (size_t)e->n * sizeof(float),
                                        (size_t)e->n * sizeof(float), (size_t)e->n, cudaMemcpyHostToDevice, e->stream));
         MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, true, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+        MDSX_CUDA(e, write_flags(e));
         MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
         e->data_set = true;
         e->sum_known = e->grad_known = false;
@@ -517,7 +609,7 @@ int mdsx_evaluate_device(mdsx_engine* e, double* d_sum, double* d_gradient) {
     DeviceGuard guard(e->device);
     int rc = enqueue_sweep(e);
     if (rc) return rc;
-    int launches = 1;
+    const int launches = e->last_launches;
     if (d_sum)
         MDSX_CUDA(e, cudaMemcpyAsync(d_sum, e->d_out + 2, sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     if (d_gradient)
@@ -527,6 +619,25 @@ int mdsx_evaluate_device(mdsx_engine* e, double* d_sum, double* d_gradient) {
     // Results live on the device; the host-side cache is refreshed lazily.
     e->sum_known = false;
     e->grad_known = true;
+    return MDSX_OK;
+}
+
+int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
+    if (!e) return MDSX_EINVAL;
+    if (schedule != MDSX_SWEEP_ROWS && schedule != MDSX_SWEEP_PAIRS)
+        return fail(e, MDSX_EINVAL, "unknown sweep schedule");
+    if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
+        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for FP32 mode and P <= 4 only");
+    if (schedule != e->schedule) {
+        e->schedule = schedule;
+        e->sum_known = e->grad_known = false;
+    }
+    return MDSX_OK;
+}
+
+int mdsx_get_sweep_schedule(mdsx_engine* e, int* out) {
+    if (!e || !out) return MDSX_EINVAL;
+    *out = e->schedule;
     return MDSX_OK;
 }
 

@@ -49,6 +49,16 @@ struct mdsx_engine {
     CUtensorMap tmap_delta{};
     CUtensorMap tmap_x[2]{};
 
+    // Unordered-pair schedule (FP32, P <= 4): plan, scratch, tensor maps per location buffer.
+    int schedule = MDSX_SWEEP_ROWS;
+    bool pairs_built = false;
+    int pair_nb = 0, pair_nc = 0, pair_grid = 0, pair_max_slots = 0;
+    long long pair_units = 0;
+    float* d_rowpart = nullptr;
+    float* d_colpart = nullptr;
+    double* d_plpart = nullptr;
+    mdsx::PairMaps pair_maps[2]{};
+
     bool data_set = false;
     double tau = 0.0, stored_tau = 0.0;
     bool sum_known = false;

@@ -1,0 +1,499 @@
+// The fused sweep over unordered pairs: FP32 mode, P <= kPairMaxP.
+//
+// d_ij = d_ji, so everything a pair needs apart from delta -- the distance,
+// 1/d, Phi(d sqrt(tau)) and phi/Phi -- is computed once per unordered pair
+// {i, j} and used for both ordered pairs (i, j) and (j, i), each with its own
+// delta_ij and delta_ji. The reference sums run over ordered pairs and delta
+// need not be symmetric (src/NewMultiDimensionalScaling.hpp:402-410 mask,
+// :421-461 gradient, :508-514 likelihood); both directions keep their own
+// residual, mask, likelihood term and gradient term. The N x N delta matrix is
+// still read once, and the transcendental work per ordered pair halves.
+//
+// Work decomposition. Columns form blocks J of 128, rows chunks I of 32. A unit
+// is one (J, I) with I at or below J's diagonal (I >= 4J): rows [32I, 32I+32) x
+// columns [128J, 128J+128), pairs i > j only. Units are numbered
+// column-block-major (J, then I = 4J .. nc-1) and CTA c of G takes the
+// contiguous range [c U / G, (c+1) U / G) (stream-K). Per unit the CTA loads
+// with TMA
+//   A   = delta[I rows][J cols]   32 x 128, plain rows
+//   B   = delta[J rows][I cols]   128 x 32, 128-byte swizzled
+//   x_I = P location rows + the flag row, 32 columns
+//   x_J = the same over J's 128 columns, with the first unit of each J
+// into a kPairStages ring (mbarrier full/empty pairs). Lane 0 of warp 0 issues
+// the copies between its own units, so all 8 warps of a CTA compute and 2 CTAs
+// of 256 threads fit an SM at 128 registers.
+//
+// Consumer warp w owns rows 4w .. 4w+3 of the chunk and lane l the columns
+// l, l+32, l+64, l+96 of the block. Rows (4w+2h, 4w+2h+1) form one f32x2 pack:
+// A gives both halves with two scalar loads of one column; B gives the packs of
+// both row pairs with one 128-bit load of row j, conflict-free because the
+// 128-byte swizzle spreads the 16-byte chunk w of rows j .. j+7 over all banks.
+//
+// Accumulation. Column gradients (the (j, i) terms) stay in registers while the
+// CTA walks the units of one J and are written per (J, CTA slot, warp) when J
+// changes; row gradients (the (i, j) terms) are summed over the warp per unit
+// and written per (unit, row). pair_finish_kernel sums both kinds of partials
+// in a fixed order, and the per-warp likelihood partials, so results are
+// bitwise reproducible from run to run. No thread waits on another CTA.
+#pragma once
+
+#include <cstdint>
+#include <cuda.h>
+
+#include "ptx.cuh"
+#include "sweep_kernel.cuh"
+
+namespace mdsx {
+
+constexpr int kPairCols = 128;  // columns per block J: 32 lanes x 4
+constexpr int kPairRows = 32;   // rows per chunk I: 8 warps x 4
+constexpr int kPairWarps = 8;
+constexpr int kPairThreads = kPairWarps * 32;
+constexpr int kPairStages = 3;
+constexpr int kPairMaxP = 4;
+constexpr int kPairFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
+
+template <int P>
+struct PairShape {
+    static constexpr int kBBytes = kPairCols * kPairRows * 4;
+    static constexpr int kABytes = kPairRows * kPairCols * 4;
+    static constexpr int kXIBytes = (P + 1) * kPairRows * 4;
+    static constexpr int kXJBytes = (P + 1) * kPairCols * 4;
+    static constexpr int kXIOffset = kBBytes + kABytes;
+    static constexpr int kXJOffset = kXIOffset + kXIBytes;
+    // stage bases stay 1024-byte aligned, as the 128-byte swizzle of B requires
+    static constexpr int kStageBytes = (kXJOffset + kXJBytes + 1023) / 1024 * 1024;
+    static constexpr int kSmemBytes = kPairStages * kStageBytes + 2 * kPairStages * 8 + 1024;
+};
+
+struct PairArgs {
+    int n;               // locations N
+    int nb;              // column blocks ceil(N / 128)
+    int nc;              // row chunks ceil(N / 32)
+    int grid;            // CTAs launched (<= n_units)
+    int max_slots;       // most CTAs meeting one column block
+    int truncation;
+    long long n_units;   // sum over J of (nc - 4J)
+    // FP32 pair constants (d-space), as in SweepArgs
+    float k_e, log2_k2;
+    float tp0, tp1, tp2, ts0, ts1, ts2;
+    double tau;
+    float* rowpart;    // [n_units][32][P]: per unit, the row sums of the (i, j) terms
+    float* colpart;    // [nb][max_slots][8][P][128]: per J, CTA slot and warp, column sums of the (j, i) terms
+    double* lpart;     // [grid][8][2]: r^2 and logPhi sums per warp
+    double* grad_out;  // [N][P]
+    double* sums_out;  // [0] r^2, [1] logPhi over ordered non-missing pairs, [2] getSumOfIncrements()
+    int* err;
+};
+
+// Units of the column blocks before J: sum over J' < J of (nc - 4 J').
+__host__ __device__ inline long long pair_units_before(int J, int nc) {
+    return (long long)J * nc - 2LL * J * (J - 1);
+}
+
+// Column block of unit u: the largest J < nb with pair_units_before(J) <= u.
+__host__ __device__ inline int pair_block_of_unit(long long u, int nb, int nc) {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pair_units_before(mid, nc) <= u)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Two unordered pairs {i, j}, {i+1, j} (one pack) in both directions. A
+// direction's residual is d - delta (negated, as in pair2_f32), its
+// coefficient c = (d - delta + E'/Phi) / d; the (i, j) term c_A (x_i - x_j)
+// accumulates into the row pack racc, the (j, i) term c_B (x_i - x_j) into the
+// column pack cacc (the sign and tau are applied by the finish kernel).
+// Fast path: 1/Phi multiplies into prod once and is counted for both
+// directions; masked path: each valid direction multiplies into prodm.
+template <int P, bool TRUNC, bool MASKED>
+__device__ __forceinline__ void pair_pack(const f2 (&xi)[P], const f2 (&nxj)[P], f2 dA, f2 dB, bool vA0, bool vA1,
+                                          bool vB0, bool vB1, const PairConstsF32& k, f2 (&racc)[P],
+                                          f2 (&cacc)[P], f2& r2, f2& prod, f2& prodm) {
+    f2 dx[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) dx[q] = fadd2(xi[q], nxj[q]);  // x_i - x_j
+    f2 d2 = fmul2(dx[0], dx[0]);
+#pragma unroll
+    for (int q = 1; q < P; ++q) d2 = ffma2(dx[q], dx[q], d2);
+    const f2 rs = rsqrt2(d2);
+    const f2 d = fmul2(d2, rs);
+    f2 nA = ffma2(dA, k.m1, d);
+    f2 nB = ffma2(dB, k.m1, d);
+    if (MASKED) {
+        nA = sel2(vA0, vA1, nA, 0.0f);
+        nB = sel2(vB0, vB1, nB, 0.0f);
+    }
+    r2 = ffma2(nA, nA, r2);
+    r2 = ffma2(nB, nB, r2);
+    f2 cA, cB;
+    if (TRUNC) {
+        const f2 e = ex2_2(ffma2(d2, k.k_e, k.log2_k2));
+        const f2 npp = ffma2(ffma2(k.ntp2, d, k.ntp1), d, k.ntp0);        // -P(d)
+        const f2 ss = ffma2(ffma2(fadd2(d, k.ts2), d, k.ts1), d, k.ts0);  // S(d)
+        const f2 aa = ffma2(e, npp, ss);                                  // S - E' P
+        const f2 iphi = fmul2(ss, rcp2(aa));                              // 1 / Phi
+        const f2 trs = fmul2(fmul2(e, iphi), rs);                         // E' / (Phi d)
+        if (MASKED) {
+            prodm = fmul2(prodm, sel2(vA0, vA1, iphi, 1.0f));
+            prodm = fmul2(prodm, sel2(vB0, vB1, iphi, 1.0f));
+        } else {
+            prod = fmul2(prod, iphi);
+        }
+        cA = ffma2(nA, rs, trs);
+        cB = ffma2(nB, rs, trs);
+    } else {
+        cA = fmul2(nA, rs);
+        cB = fmul2(nB, rs);
+    }
+    if (MASKED) {
+        cA = sel2(vA0, vA1, cA, 0.0f);
+        cB = sel2(vB0, vB1, cB, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        racc[q] = ffma2(cA, dx[q], racc[q]);
+        cacc[q] = ffma2(cB, dx[q], cacc[q]);
+    }
+}
+
+// One unit for one consumer warp: 4 rows x 4 columns per lane, both directions.
+// sA: the unit's A box; sBl: this lane's 16-byte chunk of B row `lane`
+// (swizzled); i0 = first row of the warp, j0 = first column of the block.
+template <int P, bool TRUNC, bool MASKED>
+__device__ __forceinline__ void pair_unit(const float* __restrict__ sA, const float* __restrict__ sBl,
+                                          const f2 (&xi)[2][P], const f2 (&nxj)[4][P], int i0, int j0, int n,
+                                          int lane, int wr, const PairConstsF32& k, f2 (&racc)[2][P],
+                                          f2 (&cacc)[4][P], f2& r2, f2& prod, float& l1) {
+    f2 prodm = pk(1.f, 1.f);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float4 b = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+        const int j = j0 + lane + 32 * c;
+#pragma unroll
+        for (int rp = 0; rp < 2; ++rp) {
+            const float a0 = sA[(4 * wr + 2 * rp) * kPairCols + lane + 32 * c];
+            const float a1 = sA[(4 * wr + 2 * rp + 1) * kPairCols + lane + 32 * c];
+            const float b0 = rp == 0 ? b.x : b.z;
+            const float b1 = rp == 0 ? b.y : b.w;
+            bool vA0 = true, vA1 = true, vB0 = true, vB1 = true;
+            if (MASKED) {
+                const int i = i0 + 2 * rp;
+                const bool ok0 = (i < n) && (j < n) && (i > j);
+                const bool ok1 = (i + 1 < n) && (j < n) && (i + 1 > j);
+                vA0 = ok0 && (a0 == a0);
+                vA1 = ok1 && (a1 == a1);
+                vB0 = ok0 && (b0 == b0);
+                vB1 = ok1 && (b1 == b1);
+            }
+            pair_pack<P, TRUNC, MASKED>(xi[rp], nxj[c], pk(a0, a1), pk(b0, b1), vA0, vA1, vB0, vB1, k, racc[rp],
+                                        cacc[c], r2, prod, prodm);
+        }
+    }
+    if (MASKED && TRUNC) {
+        float m0, m1;
+        upk(prodm, m0, m1);
+        l1 += lg2_approx(m0) + lg2_approx(m1);  // <= 16 factors in [1, 2] per half
+    }
+}
+
+// --------------------------------------------------------------- the kernel
+
+template <int P, bool TRUNC>
+__global__ void __launch_bounds__(kPairThreads, 2)
+    pair_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
+                const __grid_constant__ CUtensorMap tmap_xi, const __grid_constant__ CUtensorMap tmap_xj,
+                const PairArgs a) {
+    using Shape = PairShape<P>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                           ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kPairStages * Shape::kStageBytes);
+    uint64_t* empty = full + kPairStages;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long u_begin = cta_unit_begin(blockIdx.x, a.n_units, a.grid);
+    const long long u_end = cta_unit_begin(blockIdx.x + 1, a.n_units, a.grid);
+    const int K = (int)(u_end - u_begin);  // >= 1: grid <= n_units
+    const int J_first = pair_block_of_unit(u_begin, a.nb, a.nc);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kPairStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kPairWarps);
+        }
+        fence_mbar_init();
+        prefetch_tensormap(&tmap_a);
+        prefetch_tensormap(&tmap_b);
+        prefetch_tensormap(&tmap_xi);
+        prefetch_tensormap(&tmap_xj);
+    }
+    __syncthreads();
+
+    // Copy issue state (thread 0 only): next unit to issue and its (J, I).
+    const bool issuer = threadIdx.x == 0;
+    int issued = 0;
+    int pJ = J_first;
+    int pI = 4 * J_first + (int)(u_begin - pair_units_before(J_first, a.nc));
+    int pJ_loaded = -1;
+    bool issue_ok = true;
+    // Issues units up to k + 2: unit m reuses the stage of unit m - kPairStages.
+    // The stage of m <= k + 1 was released before unit k - 1 began (bounded
+    // wait); the stage of k + 2 is taken only if already free, else it is
+    // issued before the next unit.
+    auto top_up = [&](int k) {
+        while (issue_ok && issued < K && issued <= k + 2) {
+            const int m = issued;
+            const int stage = m % kPairStages;
+            if (m >= kPairStages) {
+                const uint32_t par = ((uint32_t)(m / kPairStages) & 1u) ^ 1u;
+                if (m <= k + 1) {
+                    if (!mbar_wait_bounded(&empty[stage], par, a.err, kDevTimeoutEmpty)) {
+                        issue_ok = false;
+                        break;
+                    }
+                } else if (!mbar_try_wait(&empty[stage], par)) {
+                    break;
+                }
+            }
+            unsigned char* st = smem + stage * Shape::kStageBytes;
+            const bool new_j = pJ != pJ_loaded;
+            const uint32_t bytes =
+                Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
+            mbar_arrive_expect_tx(&full[stage], bytes);
+            tma_load_2d(st, &tmap_b, pI * kPairRows, pJ * kPairCols, &full[stage]);
+            tma_load_2d(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage]);
+            tma_load_2d(st + Shape::kXIOffset, &tmap_xi, pI * kPairRows, 0, &full[stage]);
+            if (new_j) tma_load_2d(st + Shape::kXJOffset, &tmap_xj, pJ * kPairCols, 0, &full[stage]);
+            pJ_loaded = pJ;
+            if (++pI == a.nc) {
+                ++pJ;
+                pI = 4 * pJ;
+            }
+            ++issued;
+        }
+    };
+
+    const PairConstsF32 kc{pk(-1.f, -1.f),         pk(a.k_e, a.k_e), pk(a.log2_k2, a.log2_k2),
+                           pk(-a.tp0, -a.tp0),     pk(-a.tp1, -a.tp1), pk(-a.tp2, -a.tp2),
+                           pk(a.ts0, a.ts0),       pk(a.ts1, a.ts1),   pk(a.ts2, a.ts2)};
+    // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
+    // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
+    const int b_off = lane * kPairRows + ((warp ^ (lane & 7)) << 2);
+
+    f2 r2 = pk(0.f, 0.f), prod = pk(1.f, 1.f);
+    double r2_sum = 0.0, l2_twice = 0.0;  // l2_twice: log2 of 1/Phi products counted for both directions
+    float l1 = 0.f;                       // log2 of masked-path products, counted once
+    int since_fold = 0;
+    bool alive = true;
+    int k = 0;
+    for (int J = J_first; k < K && alive; ++J) {
+        const long long before = pair_units_before(J, a.nc);
+        const long long j_end = before + (a.nc - 4 * J);
+        const int k_end = (int)((u_end < j_end ? u_end : j_end) - u_begin);
+        const int slot = (int)blockIdx.x - cta_of_unit(before, a.n_units, a.grid);
+        int I = 4 * J + (int)(u_begin + k - before);
+        const int j0 = J * kPairCols;
+
+        f2 nxj[4][P];
+        f2 cacc[4][P];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < P; ++q) cacc[c][q] = pk(0.f, 0.f);
+        bool j_masked = false;
+
+        for (const int k_first = k; k < k_end; ++k, ++I) {
+            if (issuer) top_up(k);
+            const int stage = k % kPairStages;
+            if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / kPairStages) & 1u, a.err, kDevTimeoutFull)) {
+                alive = false;
+                break;
+            }
+            const float* st = reinterpret_cast<const float*>(smem + stage * Shape::kStageBytes);
+            const float* sB = st;
+            const float* sA = st + Shape::kBBytes / 4;
+            const float* sXI = st + Shape::kXIOffset / 4;
+            if (k == k_first) {
+                // x_J arrived with this unit: negated (x_j, x_j) packs and the column flags
+                const float* sXJ = st + Shape::kXJOffset / 4;
+                bool bad = false;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+#pragma unroll
+                    for (int q = 0; q < P; ++q) {
+                        const float v = -sXJ[q * kPairCols + lane + 32 * c];
+                        nxj[c][q] = pk(v, v);
+                    }
+                    bad |= sXJ[P * kPairCols + lane + 32 * c] != 0.f;
+                }
+                j_masked = __any_sync(0xffffffffu, bad);
+            }
+            f2 xi[2][P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const float4 v = *reinterpret_cast<const float4*>(sXI + q * kPairRows + 4 * warp);
+                xi[0][q] = pk(v.x, v.y);
+                xi[1][q] = pk(v.z, v.w);
+            }
+            const float4 fl = *reinterpret_cast<const float4*>(sXI + P * kPairRows + 4 * warp);
+            const bool masked =
+                j_masked || (I < 4 * J + 4) || fl.x != 0.f || fl.y != 0.f || fl.z != 0.f || fl.w != 0.f;
+            const int i0 = I * kPairRows + 4 * warp;
+
+            f2 racc[2][P];
+#pragma unroll
+            for (int rp = 0; rp < 2; ++rp)
+#pragma unroll
+                for (int q = 0; q < P; ++q) racc[rp][q] = pk(0.f, 0.f);
+            if (masked)
+                pair_unit<P, TRUNC, true>(sA, sB + b_off, xi, nxj, i0, j0, a.n, lane, warp, kc, racc, cacc, r2, prod,
+                                          l1);
+            else
+                pair_unit<P, TRUNC, false>(sA, sB + b_off, xi, nxj, i0, j0, a.n, lane, warp, kc, racc, cacc, r2,
+                                           prod, l1);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[stage]);
+
+            // row sums of this unit: rows 4w .. 4w+3, value index r * P + q
+            {
+                constexpr int KV = 4 * P;
+                using TS = TransposeShape<KV>;
+                float v[KV];
+#pragma unroll
+                for (int rp = 0; rp < 2; ++rp)
+#pragma unroll
+                    for (int q = 0; q < P; ++q) upk(racc[rp][q], v[(2 * rp) * P + q], v[(2 * rp + 1) * P + q]);
+                warp_transpose_reduce<KV>(v, lane);
+                const int idx = lane >> TS::kLaneShift;
+                if ((lane & ((1 << TS::kLaneShift) - 1)) == 0 && idx < KV)
+                    a.rowpart[((size_t)(u_begin + k) * kPairRows + 4 * warp) * P + idx] = v[0];
+            }
+
+            if (++since_fold == kPairFoldUnits) {
+                since_fold = 0;
+                float s0, s1;
+                upk(r2, s0, s1);
+                r2_sum += (double)s0 + (double)s1;
+                r2 = pk(0.f, 0.f);
+                if (TRUNC) {
+                    upk(prod, s0, s1);
+                    l2_twice += (double)(lg2_approx(s0) + lg2_approx(s1));
+                    prod = pk(1.f, 1.f);
+                }
+            }
+        }
+        if (!alive) break;
+        // column sums of block J from this CTA: [J][slot][warp][q][128]
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                a.colpart[(((size_t)J * a.max_slots + slot) * kPairWarps + warp) * (P * kPairCols) + q * kPairCols +
+                          lane + 32 * c] = sum2(cacc[c][q]);
+    }
+
+    if (issuer) {
+        // Copies still in flight (only after a failed wait): let them land before the CTA exits.
+        for (int m = k; m < issued; ++m)
+            mbar_wait_time_only(&full[m % kPairStages], (uint32_t)(m / kPairStages) & 1u);
+    }
+    if (!alive) return;
+
+    {
+        float s0, s1;
+        upk(r2, s0, s1);
+        r2_sum += (double)s0 + (double)s1;
+        if (TRUNC) {
+            upk(prod, s0, s1);
+            l2_twice += (double)(lg2_approx(s0) + lg2_approx(s1));
+        }
+    }
+    double lsum = -0.69314718055994530942 * (2.0 * l2_twice + (double)l1);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+    }
+    if (lane == 0) {
+        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 0] = r2_sum;
+        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 1] = TRUNC ? lsum : 0.0;
+    }
+}
+
+// Sums the partials of pair_kernel in a fixed order. Blocks 0 .. ceil(N P / 32)
+// - 1: 32 gradient entries each, warp w taking every 8th column block of the
+// row sums and warp w's column sums of every CTA slot; the last block: the
+// likelihood sums over CTAs and warps.
+template <int P>
+__global__ void __launch_bounds__(256) pair_finish_kernel(const PairArgs a) {
+    __shared__ double part[2][256];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long n_entries = (long long)a.n * P;
+    const int grad_blocks = (int)((n_entries + 31) / 32);
+    if ((int)blockIdx.x < grad_blocks) {
+        const long long f = (long long)blockIdx.x * 32 + lane;
+        double acc = 0.0;
+        if (f < n_entries) {
+            const int kk = (int)(f / P), q = (int)(f - (long long)kk * P);
+            const int I = kk >> 5, r = kk & 31;
+            double rs = 0.0;
+#pragma unroll 4
+            for (int J = warp; J <= (I >> 2); J += kPairWarps) {
+                const long long u = pair_units_before(J, a.nc) + (I - 4 * J);
+                rs += (double)__ldcg(&a.rowpart[((size_t)u * kPairRows + r) * P + q]);
+            }
+            const int J = kk >> 7, jj = kk & 127;
+            const long long before = pair_units_before(J, a.nc);
+            const int slots = cta_of_unit(before + (a.nc - 4 * J) - 1, a.n_units, a.grid) -
+                              cta_of_unit(before, a.n_units, a.grid) + 1;
+            double cs = 0.0;
+            for (int s = 0; s < slots; ++s)
+                cs += (double)__ldcg(&a.colpart[(((size_t)J * a.max_slots + s) * kPairWarps + warp) * (P * kPairCols) +
+                                                q * kPairCols + jj]);
+            acc = cs - rs;
+        }
+        part[0][threadIdx.x] = acc;
+        __syncthreads();
+        if (warp == 0 && f < n_entries) {
+            double t = 0.0;
+#pragma unroll
+            for (int w = 0; w < kPairWarps; ++w) t += part[0][w * 32 + lane];
+            a.grad_out[f] = a.tau * t;
+        }
+        return;
+    }
+    const int total = a.grid * kPairWarps;
+    double s0 = 0.0, s1 = 0.0;
+    for (int e = threadIdx.x; e < total; e += 256) {
+        s0 += __ldcg(&a.lpart[2 * (size_t)e]);
+        s1 += __ldcg(&a.lpart[2 * (size_t)e + 1]);
+    }
+    part[0][threadIdx.x] = s0;
+    part[1][threadIdx.x] = s1;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            part[0][threadIdx.x] += part[0][threadIdx.x + o];
+            part[1][threadIdx.x] += part[1][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double tr2 = part[0][0], tlog = part[1][0];
+        a.sums_out[0] = tr2;
+        a.sums_out[1] = tlog;
+        // src/NewMultiDimensionalScaling.hpp:198-202 and :554-557: halve the
+        // ordered-pair total; without truncation scale by 0.5 * tau.
+        a.sums_out[2] = a.truncation ? 0.5 * (0.5 * a.tau * tr2 + tlog) : 0.5 * a.tau * (0.5 * tr2);
+    }
+}
+
+}  // namespace mdsx

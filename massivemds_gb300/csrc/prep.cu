@@ -69,6 +69,12 @@ __global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int n, long lo
     }
 }
 
+__global__ void write_flag_row_kernel(const int* __restrict__ row_nan, int n, int rows_padded,
+                                      float* __restrict__ flags, int x_ld) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < x_ld; j += gridDim.x * blockDim.x)
+        flags[j] = (j >= n || (j < rows_padded && row_nan[j] != 0)) ? 1.0f : 0.0f;
+}
+
 int grid_for(long long work, int threads) {
     long long blocks = (work + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
@@ -118,6 +124,11 @@ cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, i
     else
         mark_nan_rows_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(delta), n, ld, row_nan,
                                                           rows_padded);
+    return cudaGetLastError();
+}
+
+cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, float* flags, int x_ld, cudaStream_t s) {
+    write_flag_row_kernel<<<grid_for(x_ld, 256), 256, 0, s>>>(row_nan, n, rows_padded, flags, x_ld);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,21 @@ MDSX_DECLARE_MODE(f64)
 MDSX_DECLARE_MODE(f64s32)
 #undef MDSX_DECLARE_MODE
 
+// Unordered-pair schedule (sweep_pairs.cu, pair_kernel.cuh).
+struct PairArgs;
+struct PairMaps {
+    CUtensorMap a;   // delta, box 128 columns x 32 rows
+    CUtensorMap b;   // delta, box 32 columns x 128 rows, 128-byte swizzle
+    CUtensorMap xi;  // locations + flag row, box 32 columns x (P + 1) rows
+    CUtensorMap xj;  // the same, box 128 columns x (P + 1) rows
+};
+bool pair_built(Mode mode, int p);
+cudaError_t pair_occupancy(int p, bool trunc, int* ctas_per_sm);
+// Enqueues the pair sweep and its finish kernel (two launches).
+cudaError_t pair_launch(int p, bool trunc, const PairMaps& maps, const PairArgs& args, cudaStream_t stream);
+// flags[j] = 1 for j >= n or a NaN in row j of delta (row_nan), else 0, for j < x_ld.
+cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, float* flags, int x_ld, cudaStream_t s);
+
 // Sets the message mdsx_last_error(NULL) returns on this thread (engine.cu).
 void set_global_error(const std::string& msg);
 

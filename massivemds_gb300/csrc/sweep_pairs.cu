@@ -1,0 +1,74 @@
+// Instances of the unordered-pair sweep (pair_kernel.cuh): FP32, P = 1..kPairMaxP,
+// truncation on/off, and the host-side launch of the sweep and its finish kernel.
+#include "pair_kernel.cuh"
+#include "sweep.h"
+
+namespace mdsx {
+namespace {
+
+template <int P, bool TRUNC>
+cudaError_t pair_prepare() {
+    static bool done = false;  // one engine thread at a time; idempotent if raced
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P, TRUNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         PairShape<P>::kSmemBytes);
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+template <int P, bool TRUNC>
+cudaError_t pair_launch_one(const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
+    cudaError_t e = pair_prepare<P, TRUNC>();
+    if (e != cudaSuccess) return e;
+    pair_kernel<P, TRUNC><<<args.grid, kPairThreads, PairShape<P>::kSmemBytes, stream>>>(maps.a, maps.b, maps.xi,
+                                                                                       maps.xj, args);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int blocks = (int)(((long long)args.n * P + 31) / 32) + 1;
+    pair_finish_kernel<P><<<blocks, 256, 0, stream>>>(args);
+    return cudaGetLastError();
+}
+
+template <int P, bool TRUNC>
+cudaError_t pair_occupancy_one(int* ctas) {
+    cudaError_t e = pair_prepare<P, TRUNC>();
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, pair_kernel<P, TRUNC>, kPairThreads,
+                                                         PairShape<P>::kSmemBytes);
+}
+
+template <int P>
+cudaError_t pair_launch_p(bool trunc, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
+    return trunc ? pair_launch_one<P, true>(maps, args, stream) : pair_launch_one<P, false>(maps, args, stream);
+}
+
+template <int P>
+cudaError_t pair_occupancy_p(bool trunc, int* ctas) {
+    return trunc ? pair_occupancy_one<P, true>(ctas) : pair_occupancy_one<P, false>(ctas);
+}
+
+}  // namespace
+
+bool pair_built(Mode mode, int p) { return mode == Mode::kF32 && p >= 1 && p <= kPairMaxP; }
+
+cudaError_t pair_occupancy(int p, bool trunc, int* ctas_per_sm) {
+    switch (p) {
+        case 1: return pair_occupancy_p<1>(trunc, ctas_per_sm);
+        case 2: return pair_occupancy_p<2>(trunc, ctas_per_sm);
+        case 3: return pair_occupancy_p<3>(trunc, ctas_per_sm);
+        case 4: return pair_occupancy_p<4>(trunc, ctas_per_sm);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t pair_launch(int p, bool trunc, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
+    switch (p) {
+        case 1: return pair_launch_p<1>(trunc, maps, args, stream);
+        case 2: return pair_launch_p<2>(trunc, maps, args, stream);
+        case 3: return pair_launch_p<3>(trunc, maps, args, stream);
+        case 4: return pair_launch_p<4>(trunc, maps, args, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace mdsx

@@ -127,6 +127,15 @@ class Engine:
         self._check(self._lib.mdsx_evaluate_device(self._h, ctypes.c_void_p(d_sum or 0),
                                                    ctypes.c_void_p(d_gradient or 0)))
 
+    def set_sweep_schedule(self, schedule: int) -> None:
+        """flags.SWEEP_ROWS or flags.SWEEP_PAIRS (mdsx_set_sweep_schedule)."""
+        self._check(self._lib.mdsx_set_sweep_schedule(self._h, int(schedule)))
+
+    def sweep_schedule(self) -> int:
+        out = ctypes.c_int()
+        self._check(self._lib.mdsx_get_sweep_schedule(self._h, ctypes.byref(out)))
+        return out.value
+
     def last_launch_count(self) -> int:
         out = ctypes.c_int()
         self._check(self._lib.mdsx_last_launch_count(self._h, ctypes.byref(out)))

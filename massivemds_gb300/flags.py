@@ -16,3 +16,7 @@ CUDA = 1 << 10
 DELTA_F32 = 1 << 11
 
 MAX_DIMENSION = 10
+
+# Sweep schedules (include/mdsx.h MDSX_SWEEP_*).
+SWEEP_ROWS = 0
+SWEEP_PAIRS = 1
