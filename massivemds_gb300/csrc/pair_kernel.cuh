@@ -202,6 +202,25 @@ __device__ __forceinline__ void pair_unit(const float* __restrict__ sA, const fl
     }
 }
 
+// Folds the r^2 pack and the 1/Phi product pack into compensated FP32 sums
+// (TwoSum) and resets them.
+template <bool TRUNC>
+__device__ __forceinline__ void fold_sums(f2& r2, f2& prod, float& r2_hi, float& r2_lo, float& l2_hi, float& l2_lo) {
+    float s0, s1, hi, e;
+    upk(r2, s0, s1);
+    two_sum(r2_hi, s0 + s1, hi, e);
+    r2_hi = hi;
+    r2_lo += e;
+    r2 = pk(0.f, 0.f);
+    if (TRUNC) {
+        upk(prod, s0, s1);
+        two_sum(l2_hi, lg2_approx(s0) + lg2_approx(s1), hi, e);
+        l2_hi = hi;
+        l2_lo += e;
+        prod = pk(1.f, 1.f);
+    }
+}
+
 // --------------------------------------------------------------- the kernel
 
 template <int P, bool TRUNC>
@@ -243,6 +262,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     int pI = 4 * J_first + (int)(u_begin - pair_units_before(J_first, a.nc));
     int pJ_loaded = -1;
     bool issue_ok = true;
+    const uint64_t evict_first = l2_evict_first_policy();
     // Issues units up to k + 2: unit m reuses the stage of unit m - kPairStages.
     // The stage of m <= k + 1 was released before unit k - 1 began (bounded
     // wait); the stage of k + 2 is taken only if already free, else it is
@@ -267,8 +287,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
             const uint32_t bytes =
                 Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
             mbar_arrive_expect_tx(&full[stage], bytes);
-            tma_load_2d(st, &tmap_b, pI * kPairRows, pJ * kPairCols, &full[stage]);
-            tma_load_2d(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage]);
+            // delta is read once: evict it first, keeping the partials in L2 for the finish kernel
+            tma_load_2d_hint(st, &tmap_b, pI * kPairRows, pJ * kPairCols, &full[stage], evict_first);
+            tma_load_2d_hint(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage], evict_first);
             tma_load_2d(st + Shape::kXIOffset, &tmap_xi, pI * kPairRows, 0, &full[stage]);
             if (new_j) tma_load_2d(st + Shape::kXJOffset, &tmap_xj, pJ * kPairCols, 0, &full[stage]);
             pJ_loaded = pJ;
@@ -288,8 +309,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     const int b_off = lane * kPairRows + ((warp ^ (lane & 7)) << 2);
 
     f2 r2 = pk(0.f, 0.f), prod = pk(1.f, 1.f);
-    double r2_sum = 0.0, l2_twice = 0.0;  // l2_twice: log2 of 1/Phi products counted for both directions
-    float l1 = 0.f;                       // log2 of masked-path products, counted once
+    // compensated FP32 sums (TwoSum): r^2, and log2 of 1/Phi products counted for both directions
+    float r2_hi = 0.f, r2_lo = 0.f, l2_hi = 0.f, l2_lo = 0.f;
+    float l1 = 0.f;  // log2 of masked-path products, counted once
     int since_fold = 0;
     bool alive = true;
     int k = 0;
@@ -378,15 +400,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 
             if (++since_fold == kPairFoldUnits) {
                 since_fold = 0;
-                float s0, s1;
-                upk(r2, s0, s1);
-                r2_sum += (double)s0 + (double)s1;
-                r2 = pk(0.f, 0.f);
-                if (TRUNC) {
-                    upk(prod, s0, s1);
-                    l2_twice += (double)(lg2_approx(s0) + lg2_approx(s1));
-                    prod = pk(1.f, 1.f);
-                }
+                fold_sums<TRUNC>(r2, prod, r2_hi, r2_lo, l2_hi, l2_lo);
             }
         }
         if (!alive) break;
@@ -399,6 +413,8 @@ __global__ void __launch_bounds__(kPairThreads, 2)
                           lane + 32 * c] = sum2(cacc[c][q]);
     }
 
+    // The finish kernel may be scheduled now; it waits for this grid to complete.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (issuer) {
         // Copies still in flight (only after a failed wait): let them land before the CTA exits.
         for (int m = k; m < issued; ++m)
@@ -406,16 +422,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     }
     if (!alive) return;
 
-    {
-        float s0, s1;
-        upk(r2, s0, s1);
-        r2_sum += (double)s0 + (double)s1;
-        if (TRUNC) {
-            upk(prod, s0, s1);
-            l2_twice += (double)(lg2_approx(s0) + lg2_approx(s1));
-        }
-    }
-    double lsum = -0.69314718055994530942 * (2.0 * l2_twice + (double)l1);
+    fold_sums<TRUNC>(r2, prod, r2_hi, r2_lo, l2_hi, l2_lo);
+    double r2_sum = (double)r2_hi + (double)r2_lo;
+    double lsum = -0.69314718055994530942 * (2.0 * ((double)l2_hi + (double)l2_lo) + (double)l1);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
@@ -427,72 +436,132 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     }
 }
 
-// Sums the partials of pair_kernel in a fixed order. Blocks 0 .. ceil(N P / 32)
-// - 1: 32 gradient entries each, warp w taking every 8th column block of the
-// row sums and warp w's column sums of every CTA slot; the last block: the
-// likelihood sums over CTAs and warps.
-template <int P>
-__global__ void __launch_bounds__(256) pair_finish_kernel(const PairArgs a) {
-    __shared__ double part[2][256];
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const long long n_entries = (long long)a.n * P;
-    const int grad_blocks = (int)((n_entries + 31) / 32);
-    if ((int)blockIdx.x < grad_blocks) {
-        const long long f = (long long)blockIdx.x * 32 + lane;
-        double acc = 0.0;
-        if (f < n_entries) {
-            const int kk = (int)(f / P), q = (int)(f - (long long)kk * P);
-            const int I = kk >> 5, r = kk & 31;
-            double rs = 0.0;
-#pragma unroll 4
-            for (int J = warp; J <= (I >> 2); J += kPairWarps) {
-                const long long u = pair_units_before(J, a.nc) + (I - 4 * J);
-                rs += (double)__ldcg(&a.rowpart[((size_t)u * kPairRows + r) * P + q]);
-            }
-            const int J = kk >> 7, jj = kk & 127;
-            const long long before = pair_units_before(J, a.nc);
-            const int slots = cta_of_unit(before + (a.nc - 4 * J) - 1, a.n_units, a.grid) -
-                              cta_of_unit(before, a.n_units, a.grid) + 1;
-            double cs = 0.0;
-            for (int s = 0; s < slots; ++s)
-                cs += (double)__ldcg(&a.colpart[(((size_t)J * a.max_slots + s) * kPairWarps + warp) * (P * kPairCols) +
-                                                q * kPairCols + jj]);
-            acc = cs - rs;
-        }
-        part[0][threadIdx.x] = acc;
-        __syncthreads();
-        if (warp == 0 && f < n_entries) {
-            double t = 0.0;
+// Sums the partials of pair_kernel in a fixed order. Launched as a programmatic
+// dependent of the sweep: its blocks may be scheduled while the sweep drains and
+// wait (griddepcontrol.wait) until the sweep grid has completed and its writes
+// are visible. Block 0: the likelihood sums over CTAs and warps. Block nc - I:
+// the 32 rows of chunk I (32 P outputs), thread groups g = 0 .. kGroups-1 each
+// covering all outputs for the column blocks J = g, g + kGroups, ... of the row
+// sums and the slots of the column sums; every load of a chunk is issued before
+// it is summed (the partials are spread over the buffers: the kernel is bound by
+// load latency), and the groups combine in order g = 0, 1, ...
+// Sum of K floats (K a power of two) as a fixed pairwise tree: FP32 adds
+// only, as GB300 issues few FP64 operations per clock. Compile-time levels
+// keep the array in registers.
+template <int W>
+struct TreeLevel {
+    template <int K>
+    __device__ __forceinline__ static void fold(float (&v)[K]) {
 #pragma unroll
-            for (int w = 0; w < kPairWarps; ++w) t += part[0][w * 32 + lane];
-            a.grad_out[f] = a.tau * t;
+        for (int k = 0; k < W; ++k) v[k] += v[k + W];
+        TreeLevel<W / 2>::fold(v);
+    }
+};
+template <>
+struct TreeLevel<0> {
+    template <int K>
+    __device__ __forceinline__ static void fold(float (&)[K]) {}
+};
+template <int K>
+__device__ __forceinline__ float tree_sum(float (&v)[K]) {
+    static_assert((K & (K - 1)) == 0, "K must be a power of two");
+    TreeLevel<K / 2>::fold(v);
+    return v[0];
+}
+
+template <int P>
+struct FinishShape {
+    static constexpr int kThreads = 512;
+    static constexpr int kOut = kPairRows * P;       // outputs per row chunk
+    static constexpr int kGroups = kThreads / kOut;  // P = 1: 16, 2: 8, 3: 5, 4: 4
+    static constexpr int kChunk = 8;                 // loads in flight per thread
+};
+
+template <int P>
+__global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
+    using FS = FinishShape<P>;
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    __shared__ double part[2][FS::kThreads];
+    const int t = threadIdx.x;
+    if (blockIdx.x == 0) {
+        const int total = a.grid * kPairWarps;
+        double s0 = 0.0, s1 = 0.0;
+        for (int e0 = t; e0 < total; e0 += FS::kThreads * 8) {
+            double v0[8], v1[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int e = e0 + FS::kThreads * k;
+                v0[k] = e < total ? __ldcg(&a.lpart[2 * (size_t)e]) : 0.0;
+                v1[k] = e < total ? __ldcg(&a.lpart[2 * (size_t)e + 1]) : 0.0;
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                s0 += v0[k];
+                s1 += v1[k];
+            }
+        }
+        part[0][t] = s0;
+        part[1][t] = s1;
+        __syncthreads();
+        for (int o = FS::kThreads / 2; o > 0; o >>= 1) {
+            if (t < o) {
+                part[0][t] += part[0][t + o];
+                part[1][t] += part[1][t + o];
+            }
+            __syncthreads();
+        }
+        if (t == 0) {
+            const double tr2 = part[0][0], tlog = part[1][0];
+            a.sums_out[0] = tr2;
+            a.sums_out[1] = tlog;
+            // src/NewMultiDimensionalScaling.hpp:198-202 and :554-557: halve the
+            // ordered-pair total; without truncation scale by 0.5 * tau.
+            a.sums_out[2] = a.truncation ? 0.5 * (0.5 * a.tau * tr2 + tlog) : 0.5 * a.tau * (0.5 * tr2);
         }
         return;
     }
-    const int total = a.grid * kPairWarps;
-    double s0 = 0.0, s1 = 0.0;
-    for (int e = threadIdx.x; e < total; e += 256) {
-        s0 += __ldcg(&a.lpart[2 * (size_t)e]);
-        s1 += __ldcg(&a.lpart[2 * (size_t)e + 1]);
-    }
-    part[0][threadIdx.x] = s0;
-    part[1][threadIdx.x] = s1;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            part[0][threadIdx.x] += part[0][threadIdx.x + o];
-            part[1][threadIdx.x] += part[1][threadIdx.x + o];
+    const int I = a.nc - (int)blockIdx.x;  // the chunks with the most partials are scheduled first
+    const int g = t / FS::kOut, o = t - g * FS::kOut;  // o = r * P + q
+    double acc = 0.0;
+    if (g < FS::kGroups) {
+        // row sums: units (J, I), J = 0 .. I/4, each [32 rows][P] contiguous
+        const int j_max = I >> 2;
+        for (int J0 = g; J0 <= j_max; J0 += FS::kGroups * FS::kChunk) {
+            float v[FS::kChunk];
+#pragma unroll
+            for (int k = 0; k < FS::kChunk; ++k) {
+                const int J = J0 + FS::kGroups * k;
+                const long long u = pair_units_before(J, a.nc) + (I - 4 * J);
+                v[k] = J <= j_max ? __ldcg(&a.rowpart[(size_t)u * FS::kOut + o]) : 0.f;
+            }
+            acc -= (double)tree_sum<FS::kChunk>(v);
         }
-        __syncthreads();
+        // column sums of block J = I/4 for its rows (I % 4) * 32 + r: entries (slot, warp)
+        const int J = I >> 2, r = o / P, q = o - r * P, jj = (I & 3) * kPairRows + r;
+        const long long before = pair_units_before(J, a.nc);
+        const int n_e = (cta_of_unit(before + (a.nc - 4 * J) - 1, a.n_units, a.grid) -
+                         cta_of_unit(before, a.n_units, a.grid) + 1) *
+                        kPairWarps;
+        for (int e0 = g; e0 < n_e; e0 += FS::kGroups * 8) {
+            float v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int e = e0 + FS::kGroups * k;  // slot e / 8, warp e % 8
+                v[k] = e < n_e ? __ldcg(&a.colpart[((size_t)J * a.max_slots * kPairWarps + e) * (P * kPairCols) +
+                                                   q * kPairCols + jj])
+                               : 0.f;
+            }
+            acc += (double)tree_sum<8>(v);
+        }
     }
-    if (threadIdx.x == 0) {
-        const double tr2 = part[0][0], tlog = part[1][0];
-        a.sums_out[0] = tr2;
-        a.sums_out[1] = tlog;
-        // src/NewMultiDimensionalScaling.hpp:198-202 and :554-557: halve the
-        // ordered-pair total; without truncation scale by 0.5 * tau.
-        a.sums_out[2] = a.truncation ? 0.5 * (0.5 * a.tau * tr2 + tlog) : 0.5 * a.tau * (0.5 * tr2);
+    part[0][t] = acc;
+    __syncthreads();
+    if (t < FS::kOut) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < FS::kGroups; ++k) s += part[0][k * FS::kOut + t];
+        const int row = I * kPairRows + t / P;
+        if (row < a.n) a.grad_out[(size_t)I * FS::kOut + t] = a.tau * s;
     }
 }
 

@@ -24,9 +24,19 @@ cudaError_t pair_launch_one(const PairMaps& maps, const PairArgs& args, cudaStre
                                                                                        maps.xj, args);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const int blocks = (int)(((long long)args.n * P + 31) / 32) + 1;
-    pair_finish_kernel<P><<<blocks, 256, 0, stream>>>(args);
-    return cudaGetLastError();
+    // the finish kernel as a programmatic dependent: launched while the sweep
+    // drains, it waits in griddepcontrol.wait for the sweep's results
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)args.nc + 1);
+    cfg.blockDim = dim3(FinishShape<P>::kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, pair_finish_kernel<P>, args);
 }
 
 template <int P, bool TRUNC>
