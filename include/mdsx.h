@@ -141,7 +141,8 @@ int mdsx_last_launch_count(mdsx_engine* engine, int* out);
  *   MDSX_SWEEP_PAIRS - each unordered pair {i, j} once: distance and Phi shared
  *                      by (i, j) and (j, i), each direction with its own delta;
  *                      a sweep kernel plus a finish kernel. FP32 mode, P <= 4.
- * New engines use MDSX_SWEEP_PAIRS where it is built, else MDSX_SWEEP_ROWS.
+ * New engines use MDSX_SWEEP_PAIRS where it is built and truncation is on (the
+ * pair math dominates there), else MDSX_SWEEP_ROWS.
  * Setting MDSX_SWEEP_PAIRS where it is not built returns MDSX_EUNSUPPORTED. */
 #define MDSX_SWEEP_ROWS 0
 #define MDSX_SWEEP_PAIRS 1

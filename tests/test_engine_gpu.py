@@ -7,7 +7,7 @@ Tolerances (from the engine's stated targets):
   FP32 mode (FP32 pairs, compensated FP32 partials, FP64 reductions): within
     1e-5 relative of the FP64 oracle on the same (FP32-rounded) delta, with
     either sweep schedule: "f32" is the engine's default (unordered pairs for
-    P <= 4), "f32rows" forces the ordered-pair row-block schedule.
+    P <= 4 with truncation, else row blocks), "f32rows" and "f32pairs" force one.
 """
 import numpy as np
 import pytest
@@ -33,10 +33,12 @@ def grad_rel(g, ref):
 
 def make_engine(n, p, trunc, mode, delta, x, tau):
     fl = F.LEFT_TRUNCATION if trunc else 0
-    fl |= {"f64": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f64s32": F.DELTA_F32}[mode]
+    fl |= {"f64": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f32pairs": F.FLOAT, "f64s32": F.DELTA_F32}[mode]
     e = Engine(p, n, fl)
     if mode == "f32rows":
         e.set_sweep_schedule(F.SWEEP_ROWS)
+    if mode == "f32pairs":
+        e.set_sweep_schedule(F.SWEEP_PAIRS)
     e.setPairwiseData(delta)
     e.updateLocations(-1, x)
     e.setParameters([tau])
@@ -45,11 +47,11 @@ def make_engine(n, p, trunc, mode, delta, x, tau):
 
 
 def oracle_delta(delta, mode):
-    return delta.astype(np.float32) if mode in ("f32", "f32rows", "f64s32") else delta
+    return delta.astype(np.float32) if mode in ("f32", "f32rows", "f32pairs", "f64s32") else delta
 
 
 def tolerances(mode):
-    return (TOL_F32, TOL_F32) if mode in ("f32", "f32rows") else (TOL_F64_SUM, TOL_F64_GRAD)
+    return (TOL_F32, TOL_F32) if mode in ("f32", "f32rows", "f32pairs") else (TOL_F64_SUM, TOL_F64_GRAD)
 
 
 # ------------------------------------------------------------- golden vectors
@@ -121,7 +123,7 @@ def _inputs(n, p, seed, nans=0, asym=False):
     return delta, rng.standard_normal((n, p))
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32", "f32rows", "f64s32"])
+@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32"])
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 31, 32, 33, 127, 128, 129, 159, 160, 161, 257, 385, 1000])
 def test_sizes_and_edges(mode, n):
     p, tau = 2, 1.7
@@ -141,9 +143,11 @@ def test_sizes_and_edges(mode, n):
         assert grad_rel(g, g_ref) < tol_g, trunc
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32", "f32rows"])
+@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs"])
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_dimensions(mode, p):
+    if mode == "f32pairs" and p > 4:
+        pytest.skip("the unordered-pair schedule is built for P <= 4")
     n, tau = 300, 0.8
     delta, x = _inputs(n, p, seed=100 + p, nans=2, asym=True)
     tol_s, tol_g = tolerances(mode)
@@ -162,7 +166,7 @@ def test_nan_rows_and_asymmetric_delta():
     delta[5, :] = np.nan       # a whole row missing
     delta[:, 9] = np.nan       # a whole column missing
     delta[100, 101] = np.nan
-    for mode in ("f64", "f32", "f32rows"):
+    for mode in ("f64", "f32rows", "f32pairs"):
         tol_s, tol_g = tolerances(mode)
         e = make_engine(n, p, True, mode, delta, x, tau)
         s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -178,7 +182,7 @@ def test_precision_extremes():
     n, p = 500, 2
     delta, x = _inputs(n, p, seed=9)
     for tau in (1e-3, 0.05, 40.0, 900.0):
-        for mode in ("f64", "f32", "f32rows"):
+        for mode in ("f64", "f32rows", "f32pairs"):
             tol_s, tol_g = tolerances(mode)
             e = make_engine(n, p, True, mode, delta, x, tau)
             s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -235,7 +239,7 @@ def test_restore_returns_stored_sum_without_sweep():
 def test_deterministic_bitwise():
     n, p, tau = 3000, 2, 2.0
     delta, x = _inputs(n, p, seed=13)
-    for mode in ("f32", "f32rows", "f64"):
+    for mode in ("f32rows", "f32pairs", "f64"):
         e = make_engine(n, p, True, mode, delta, x, tau)
         s1, g1 = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
         e.makeDirty()
@@ -288,10 +292,17 @@ def test_error_statuses():
 
 
 def test_sweep_schedules():
-    """FP32 engines with P <= 4 default to the unordered-pair schedule (sweep +
-    finish kernel); other modes and dimensions run the row-block schedule and
-    refuse the pair schedule; switching invalidates the cached results."""
+    """Truncated FP32 engines with P <= 4 default to the unordered-pair schedule
+    (sweep + finish kernel), untruncated ones to the row-block schedule; other
+    modes and dimensions run the row-block schedule and refuse the pair schedule;
+    switching invalidates the cached results."""
     n, tau = 300, 1.3
+    delta, x = _inputs(n, 2, seed=29)
+    e = make_engine(n, 2, False, "f32", delta, x, tau)
+    assert e.sweep_schedule() == F.SWEEP_ROWS
+    e.set_sweep_schedule(F.SWEEP_PAIRS)
+    assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
+    e.close()
     for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (5, "f32", F.SWEEP_ROWS),
                              (2, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_ROWS)):
         delta, x = _inputs(n, p, seed=30 + p)
@@ -329,7 +340,7 @@ def test_pair_schedule_symmetric_pairs_and_missing_blocks():
             delta[i, j] = np.nan  # (j, i) stays observed
         delta[n // 2, :] = np.nan
         for trunc in (True, False):
-            e = make_engine(n, p, trunc, "f32", delta, x, tau)
+            e = make_engine(n, p, trunc, "f32pairs", delta, x, tau)
             assert e.sweep_schedule() == F.SWEEP_PAIRS
             s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
             e.close()
@@ -344,7 +355,7 @@ def test_device_api_matches_host_api():
     torch = pytest.importorskip("torch")
     n, p, tau = 700, 2, 2.0
     delta, x = _inputs(n, p, seed=16)
-    for mode in ("f32", "f32rows", "f64"):
+    for mode in ("f32rows", "f32pairs", "f64"):
         e = make_engine(n, p, True, mode, delta, x, tau)
         s_host, g_host = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
         dx = torch.tensor(x, dtype=torch.float64, device="cuda")
@@ -372,7 +383,7 @@ def n20000():
     return delta, x, tau, oracle.sum_of_increments(delta, x, tau), oracle.gradient(delta, x, tau)
 
 
-@pytest.mark.parametrize("mode", ["f32", "f32rows", "f64s32"])
+@pytest.mark.parametrize("mode", ["f32rows", "f32pairs", "f64s32"])
 def test_full_size_n20000(mode, n20000):
     """The N=20 000, P=2, tau=2 workload with FP32-stored delta: one evaluation
     against the FP64 oracle on the same FP32 delta."""
