@@ -57,6 +57,9 @@ struct mdsx_engine {
     float* d_rowpart = nullptr;
     float* d_colpart = nullptr;
     double* d_plpart = nullptr;
+    long long* d_pair_begin = nullptr;  // [pair_grid + 1]
+    int* d_pair_jfirst = nullptr;       // [pair_nb]
+    int* d_pair_jslots = nullptr;       // [pair_nb]
     mdsx::PairMaps pair_maps[2]{};
 
     bool data_set = false;

@@ -13,7 +13,9 @@
 // is one (J, I) with I at or below J's diagonal (I >= 4J): rows [32I, 32I+32) x
 // columns [128J, 128J+128), pairs i > j only. Units are numbered
 // column-block-major (J, then I = 4J .. nc-1) and CTA c of G takes the
-// contiguous range [c U / G, (c+1) U / G) (stream-K). Per unit the CTA loads
+// contiguous range of units whose modelled cost is 1/G of the total (stream-K;
+// the host weights diagonal units and column-block starts, see
+// pair_unit_cost). Per unit the CTA loads
 // with TMA
 //   A   = delta[I rows][J cols]   32 x 128, plain rows
 //   B   = delta[J rows][I cols]   128 x 32, 128-byte swizzled
@@ -81,6 +83,9 @@ struct PairArgs {
     float* rowpart;    // [n_units][32][P]: per unit, the row sums of the (i, j) terms
     float* colpart;    // [nb][max_slots][8][P][128]: per J, CTA slot and warp, column sums of the (j, i) terms
     double* lpart;     // [grid][8][2]: r^2 and logPhi sums per warp
+    const long long* cta_begin;  // [grid + 1]: CTA c takes units [cta_begin[c], cta_begin[c+1])
+    const int* j_first_cta;      // [nb]: first CTA whose range meets column block J
+    const int* j_slots;          // [nb]: CTAs whose ranges meet column block J
     double* grad_out;  // [N][P]
     double* sums_out;  // [0] r^2, [1] logPhi over ordered non-missing pairs, [2] getSumOfIncrements()
     int* err;
@@ -89,6 +94,22 @@ struct PairArgs {
 // Units of the column blocks before J: sum over J' < J of (nc - 4 J').
 __host__ __device__ inline long long pair_units_before(int J, int nc) {
     return (long long)J * nc - 2LL * J * (J - 1);
+}
+
+// Modelled cost of the units of one column block, used by the host to split
+// the units over CTAs: a unit costs 1, a diagonal unit (I < 4J + 4, masked
+// path) kPairDiagExtra more, and the first unit of a block kPairBlockExtra
+// more (column flush, x_J reload).
+#ifndef MDSX_PAIR_DIAG_EXTRA
+#define MDSX_PAIR_DIAG_EXTRA 0.6
+#endif
+#ifndef MDSX_PAIR_BLOCK_EXTRA
+#define MDSX_PAIR_BLOCK_EXTRA 0.2
+#endif
+constexpr double kPairDiagExtra = MDSX_PAIR_DIAG_EXTRA;
+constexpr double kPairBlockExtra = MDSX_PAIR_BLOCK_EXTRA;
+__host__ __device__ inline double pair_unit_cost(int I, int J) {
+    return 1.0 + (I < 4 * J + 4 ? kPairDiagExtra : 0.0) + (I == 4 * J ? kPairBlockExtra : 0.0);
 }
 
 // Column block of unit u: the largest J < nb with pair_units_before(J) <= u.
@@ -237,9 +258,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const long long u_begin = cta_unit_begin(blockIdx.x, a.n_units, a.grid);
-    const long long u_end = cta_unit_begin(blockIdx.x + 1, a.n_units, a.grid);
-    const int K = (int)(u_end - u_begin);  // >= 1: grid <= n_units
+    const long long u_begin = a.cta_begin[blockIdx.x];
+    const long long u_end = a.cta_begin[blockIdx.x + 1];
+    const int K = (int)(u_end - u_begin);  // >= 1: the host keeps every range non-empty
     const int J_first = pair_block_of_unit(u_begin, a.nb, a.nc);
 
     if (threadIdx.x == 0) {
@@ -319,7 +340,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
         const long long before = pair_units_before(J, a.nc);
         const long long j_end = before + (a.nc - 4 * J);
         const int k_end = (int)((u_end < j_end ? u_end : j_end) - u_begin);
-        const int slot = (int)blockIdx.x - cta_of_unit(before, a.n_units, a.grid);
+        const int slot = (int)blockIdx.x - a.j_first_cta[J];
         int I = 4 * J + (int)(u_begin + k - before);
         const int j0 = J * kPairCols;
 
@@ -539,9 +560,7 @@ __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
         // column sums of block J = I/4 for its rows (I % 4) * 32 + r: entries (slot, warp)
         const int J = I >> 2, r = o / P, q = o - r * P, jj = (I & 3) * kPairRows + r;
         const long long before = pair_units_before(J, a.nc);
-        const int n_e = (cta_of_unit(before + (a.nc - 4 * J) - 1, a.n_units, a.grid) -
-                         cta_of_unit(before, a.n_units, a.grid) + 1) *
-                        kPairWarps;
+        const int n_e = a.j_slots[J] * kPairWarps;
         for (int e0 = g; e0 < n_e; e0 += FS::kGroups * 8) {
             float v[8];
 #pragma unroll
