@@ -115,7 +115,8 @@ void free_all(mdsx_engine* e) {
 // delta (plain and 128-byte swizzled boxes) and of both location buffers.
 int plan_pairs(mdsx_engine* e) {
     int ctas = 0;
-    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, &ctas));
+    const bool f64 = !e->x_f32;
+    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, f64, &ctas));
     if (ctas < 1) return fail(e, MDSX_ECUDA, "pair sweep kernel cannot be resident on this device");
     e->pair_nb = (e->n + mdsx::kPairCols - 1) / mdsx::kPairCols;
     e->pair_nc = (e->n + mdsx::kPairRows - 1) / mdsx::kPairRows;
@@ -164,9 +165,10 @@ int plan_pairs(mdsx_engine* e) {
                             cudaMemcpyHostToDevice));
     MDSX_CUDA(e, cudaMemcpy(e->d_pair_jfirst, jfirst.data(), (size_t)e->pair_nb * sizeof(int), cudaMemcpyHostToDevice));
     MDSX_CUDA(e, cudaMemcpy(e->d_pair_jslots, jslots.data(), (size_t)e->pair_nb * sizeof(int), cudaMemcpyHostToDevice));
-    MDSX_CUDA(e, cudaMalloc(&e->d_rowpart, (size_t)e->pair_units * mdsx::kPairRows * e->p * sizeof(float)));
+    const size_t part_bytes = f64 ? sizeof(double) : sizeof(float);
+    MDSX_CUDA(e, cudaMalloc(&e->d_rowpart, (size_t)e->pair_units * mdsx::kPairRows * e->p * part_bytes));
     MDSX_CUDA(e, cudaMalloc(&e->d_colpart, (size_t)e->pair_nb * e->pair_max_slots * mdsx::kPairWarps * e->p *
-                                               mdsx::kPairCols * sizeof(float)));
+                                               mdsx::kPairCols * part_bytes));
     MDSX_CUDA(e, cudaMalloc(&e->d_plpart, (size_t)e->pair_grid * mdsx::kPairWarps * 2 * sizeof(double)));
     for (int b = 0; b < 2; ++b) {
         mdsx::PairMaps& m = e->pair_maps[b];
@@ -176,9 +178,9 @@ int plan_pairs(mdsx_engine* e) {
                               CU_TENSOR_MAP_SWIZZLE_128B);
         // the location maps span x_ld columns, so the flags of rows >= N are read from memory (1), not filled
         if (!rc)
-            rc = make_tmap_2d(e, &m.xi, e->d_x[b], true, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairRows, e->p + 1);
+            rc = make_tmap_2d(e, &m.xi, e->d_x[b], e->x_f32, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairRows, e->p + 1);
         if (!rc)
-            rc = make_tmap_2d(e, &m.xj, e->d_x[b], true, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairCols, e->p + 1);
+            rc = make_tmap_2d(e, &m.xj, e->d_x[b], e->x_f32, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairCols, e->p + 1);
         if (rc) return rc;
     }
     return MDSX_OK;
@@ -251,13 +253,13 @@ int plan_and_allocate(mdsx_engine* e) {
     return MDSX_OK;
 }
 
-// Flag row (row P) of both FP32 location buffers from the NaN-row marks.
+// Flag row (row P) of both location buffers from the NaN-row marks.
 cudaError_t write_flags(mdsx_engine* e) {
-    if (!e->x_f32) return cudaSuccess;
+    const size_t elem = e->x_f32 ? sizeof(float) : sizeof(double);
     for (int b = 0; b < 2; ++b) {
         cudaError_t err = mdsx::write_flag_row(e->d_row_nan, e->n, e->rows_padded,
-                                               static_cast<float*>(e->d_x[b]) + (size_t)e->p * e->x_ld, e->x_ld,
-                                               e->stream);
+                                               static_cast<char*>(e->d_x[b]) + (size_t)e->p * e->x_ld * elem,
+                                               e->x_f32, e->x_ld, e->stream);
         if (err != cudaSuccess) return err;
     }
     return cudaSuccess;
@@ -331,6 +333,7 @@ int enqueue_sweep(mdsx_engine* e) {
         pa.ts1 = a.ts1;
         pa.ts2 = a.ts2;
         pa.tau = a.tau;
+        pa.sqrt_tau = a.sqrt_tau;
         pa.rowpart = e->d_rowpart;
         pa.colpart = e->d_colpart;
         pa.lpart = e->d_plpart;
@@ -340,7 +343,7 @@ int enqueue_sweep(mdsx_engine* e) {
         pa.grad_out = a.grad_out;
         pa.sums_out = a.sums_out;
         pa.err = a.err;
-        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->pair_maps[e->xcur], pa, e->stream));
+        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, !e->x_f32, e->pair_maps[e->xcur], pa, e->stream));
         e->last_launches = 2;
         return MDSX_OK;
     }
@@ -671,7 +674,8 @@ int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
     if (schedule != MDSX_SWEEP_ROWS && schedule != MDSX_SWEEP_PAIRS)
         return fail(e, MDSX_EINVAL, "unknown sweep schedule");
     if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
-        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for FP32 mode and P <= 4 only");
+        return fail(e, MDSX_EUNSUPPORTED,
+                    "the unordered-pair schedule is built for FP32 and DELTA_F32 modes and P <= 4 only");
     if (schedule != e->schedule) {
         e->schedule = schedule;
         e->sum_known = e->grad_known = false;

@@ -54,8 +54,8 @@ struct mdsx_engine {
     bool pairs_built = false;
     int pair_nb = 0, pair_nc = 0, pair_grid = 0, pair_max_slots = 0;
     long long pair_units = 0;
-    float* d_rowpart = nullptr;
-    float* d_colpart = nullptr;
+    void* d_rowpart = nullptr;  // float (FP32 math) or double (FP64 math)
+    void* d_colpart = nullptr;
     double* d_plpart = nullptr;
     long long* d_pair_begin = nullptr;  // [pair_grid + 1]
     int* d_pair_jfirst = nullptr;       // [pair_nb]

@@ -1,4 +1,5 @@
-// The fused sweep over unordered pairs: FP32 mode, P <= kPairMaxP.
+// The fused sweep over unordered pairs: FP32 pair math (FP32 mode), or FP64
+// pair math over FP32-stored delta (DELTA_F32 mode), P <= kPairMaxP.
 //
 // d_ij = d_ji, so everything a pair needs apart from delta -- the distance,
 // 1/d, Phi(d sqrt(tau)) and phi/Phi -- is computed once per unordered pair
@@ -12,24 +13,24 @@
 // Work decomposition. Columns form blocks J of 128, rows chunks I of 32. A unit
 // is one (J, I) with I at or below J's diagonal (I >= 4J): rows [32I, 32I+32) x
 // columns [128J, 128J+128), pairs i > j only. Units are numbered
-// column-block-major (J, then I = 4J .. nc-1) and CTA c of G takes the
+// column-block-major (J, then I = 4J .. nc-1) and CTA c of G takes a
 // contiguous range of units whose modelled cost is 1/G of the total (stream-K;
 // the host weights diagonal units and column-block starts, see
-// pair_unit_cost). Per unit the CTA loads
-// with TMA
-//   A   = delta[I rows][J cols]   32 x 128, plain rows
-//   B   = delta[J rows][I cols]   128 x 32, 128-byte swizzled
-//   x_I = P location rows + the flag row, 32 columns
+// pair_unit_cost). Per unit the CTA loads with TMA
+//   A   = delta[I rows][J cols]   32 x 128 FP32, plain rows
+//   B   = delta[J rows][I cols]   128 x 32 FP32, 128-byte swizzled
+//   x_I = P location rows + the flag row, 32 columns (compute type)
 //   x_J = the same over J's 128 columns, with the first unit of each J
-// into a kPairStages ring (mbarrier full/empty pairs). Lane 0 of warp 0 issues
-// the copies between its own units, so all 8 warps of a CTA compute and 2 CTAs
-// of 256 threads fit an SM at 128 registers.
+// into a ring of PairShape::kStages stages (mbarrier full/empty pairs). Lane 0
+// of warp 0 issues the copies between its own units, so all 8 warps of a CTA
+// compute and 2 CTAs of 256 threads fit an SM at 128 registers.
 //
 // Consumer warp w owns rows 4w .. 4w+3 of the chunk and lane l the columns
-// l, l+32, l+64, l+96 of the block. Rows (4w+2h, 4w+2h+1) form one f32x2 pack:
-// A gives both halves with two scalar loads of one column; B gives the packs of
-// both row pairs with one 128-bit load of row j, conflict-free because the
-// 128-byte swizzle spreads the 16-byte chunk w of rows j .. j+7 over all banks.
+// l, l+32, l+64, l+96 of the block. B gives a lane its four rows of column j
+// with one 128-bit load of row j, conflict-free because the 128-byte swizzle
+// spreads the 16-byte chunk w of rows j .. j+7 over all banks. The math policy
+// (PairMathF32: f32x2 packs of two rows; PairMathF64: scalar FP64) does the
+// pairs and keeps the likelihood sums.
 //
 // Accumulation. Column gradients (the (j, i) terms) stay in registers while the
 // CTA walks the units of one J and are written per (J, CTA slot, warp) when J
@@ -51,21 +52,22 @@ constexpr int kPairCols = 128;  // columns per block J: 32 lanes x 4
 constexpr int kPairRows = 32;   // rows per chunk I: 8 warps x 4
 constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
-constexpr int kPairStages = 3;
 constexpr int kPairMaxP = 4;
-constexpr int kPairFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
 
-template <int P>
+// XB: bytes per location element (4: FP32 math, 8: FP64 math). FP64 math is
+// bound by the FP64 pipe, so two stages hide the copies; FP32 math gets three.
+template <int P, int XB>
 struct PairShape {
+    static constexpr int kStages = XB == 4 ? 3 : 2;
     static constexpr int kBBytes = kPairCols * kPairRows * 4;
     static constexpr int kABytes = kPairRows * kPairCols * 4;
-    static constexpr int kXIBytes = (P + 1) * kPairRows * 4;
-    static constexpr int kXJBytes = (P + 1) * kPairCols * 4;
+    static constexpr int kXIBytes = (P + 1) * kPairRows * XB;
+    static constexpr int kXJBytes = (P + 1) * kPairCols * XB;
     static constexpr int kXIOffset = kBBytes + kABytes;
     static constexpr int kXJOffset = kXIOffset + kXIBytes;
     // stage bases stay 1024-byte aligned, as the 128-byte swizzle of B requires
     static constexpr int kStageBytes = (kXJOffset + kXJBytes + 1023) / 1024 * 1024;
-    static constexpr int kSmemBytes = kPairStages * kStageBytes + 2 * kPairStages * 8 + 1024;
+    static constexpr int kSmemBytes = kStages * kStageBytes + 2 * kStages * 8 + 1024;
 };
 
 struct PairArgs {
@@ -79,9 +81,9 @@ struct PairArgs {
     // FP32 pair constants (d-space), as in SweepArgs
     float k_e, log2_k2;
     float tp0, tp1, tp2, ts0, ts1, ts2;
-    double tau;
-    float* rowpart;    // [n_units][32][P]: per unit, the row sums of the (i, j) terms
-    float* colpart;    // [nb][max_slots][8][P][128]: per J, CTA slot and warp, column sums of the (j, i) terms
+    double tau, sqrt_tau;
+    void* rowpart;     // [n_units][32][P]: per unit, the row sums of the (i, j) terms (partial type)
+    void* colpart;     // [nb][max_slots][8][P][128]: per J, CTA slot and warp, column sums of the (j, i) terms
     double* lpart;     // [grid][8][2]: r^2 and logPhi sums per warp
     const long long* cta_begin;  // [grid + 1]: CTA c takes units [cta_begin[c], cta_begin[c+1])
     const int* j_first_cta;      // [nb]: first CTA whose range meets column block J
@@ -124,6 +126,8 @@ __host__ __device__ inline int pair_block_of_unit(long long u, int nb, int nc) {
     }
     return lo;
 }
+
+// ------------------------------------------------------------ FP32 pair math
 
 // Two unordered pairs {i, j}, {i+1, j} (one pack) in both directions. A
 // direction's residual is d - delta (negated, as in pair2_f32), its
@@ -242,19 +246,233 @@ __device__ __forceinline__ void fold_sums(f2& r2, f2& prod, float& r2_hi, float&
     }
 }
 
+// FP32 policy: f32x2 packs of two rows (pair_unit); FP32 partials; r^2 and
+// log2 of the 1/Phi products folded every kFoldUnits units into compensated
+// FP32 sums (TwoSum).
+template <int P, bool TRUNC>
+struct PairMathF32 {
+    using X = float;     // location element in shared memory
+    using Part = float;  // row and column partials
+    static constexpr int kFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
+    struct Cols {        // one column block: negated (x_j, x_j) packs and the column sums
+        f2 nxj[4][P];
+        f2 acc[4][P];
+    };
+    struct Sums {
+        f2 r2, prod;
+        float r2_hi, r2_lo, l2_hi, l2_lo;  // l2: log2 of 1/Phi products counted for both directions
+        float l1;                          // log2 of masked-path products, counted once
+        int since_fold;
+    };
+    PairConstsF32 k;
+
+    __device__ explicit PairMathF32(const PairArgs& a)
+        : k{pk(-1.f, -1.f),     pk(a.k_e, a.k_e),   pk(a.log2_k2, a.log2_k2), pk(-a.tp0, -a.tp0), pk(-a.tp1, -a.tp1),
+            pk(-a.tp2, -a.tp2), pk(a.ts0, a.ts0), pk(a.ts1, a.ts1),         pk(a.ts2, a.ts2)} {}
+
+    __device__ static void init(Sums& s) {
+        s.r2 = pk(0.f, 0.f);
+        s.prod = pk(1.f, 1.f);
+        s.r2_hi = s.r2_lo = s.l2_hi = s.l2_lo = s.l1 = 0.f;
+        s.since_fold = 0;
+    }
+    __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const float v = -sXJ[q * kPairCols + lane + 32 * c];
+                cols.nxj[c][q] = pk(v, v);
+                cols.acc[c][q] = pk(0.f, 0.f);
+            }
+    }
+    // One unit: v[r * P + q] = this lane's sum of the (i, j) terms of row 4w + r.
+    template <bool MASKED>
+    __device__ void unit(const float* sA, const float* sBl, const X* sXI, Cols& cols, Sums& s, int i0, int j0,
+                         int n, int lane, int warp, Part (&v)[4 * P]) const {
+        f2 xi[2][P], racc[2][P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const float4 x4 = *reinterpret_cast<const float4*>(sXI + q * kPairRows + 4 * warp);
+            xi[0][q] = pk(x4.x, x4.y);
+            xi[1][q] = pk(x4.z, x4.w);
+            racc[0][q] = racc[1][q] = pk(0.f, 0.f);
+        }
+        pair_unit<P, TRUNC, MASKED>(sA, sBl, xi, cols.nxj, i0, j0, n, lane, warp, k, racc, cols.acc, s.r2, s.prod,
+                                    s.l1);
+#pragma unroll
+        for (int rp = 0; rp < 2; ++rp)
+#pragma unroll
+            for (int q = 0; q < P; ++q) upk(racc[rp][q], v[(2 * rp) * P + q], v[(2 * rp + 1) * P + q]);
+    }
+    __device__ static void after_unit(Sums& s) {
+        if (++s.since_fold == kFoldUnits) {
+            s.since_fold = 0;
+            fold_sums<TRUNC>(s.r2, s.prod, s.r2_hi, s.r2_lo, s.l2_hi, s.l2_lo);
+        }
+    }
+    __device__ static Part col_value(const Cols& cols, int c, int q) { return sum2(cols.acc[c][q]); }
+    // Sum of r^2 and of log Phi (natural) over this lane's ordered pairs.
+    __device__ static void result(Sums& s, double& r2, double& lsum) {
+        fold_sums<TRUNC>(s.r2, s.prod, s.r2_hi, s.r2_lo, s.l2_hi, s.l2_lo);
+        r2 = (double)s.r2_hi + (double)s.r2_lo;
+        lsum = TRUNC ? -0.69314718055994530942 * (2.0 * ((double)s.l2_hi + (double)s.l2_lo) + (double)s.l1) : 0.0;
+    }
+};
+
+// ------------------------------------------------------------ FP64 pair math
+
+// One unordered pair {i, j} in FP64 (CUDA double rsqrt, erfc, exp; one
+// division), both directions: dA = delta_ij, dB = delta_ji (FP32-stored).
+// With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
+// -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
+// into cacc (signs as in the FP32 policy). Fast path: Phi multiplies into prod
+// once and counts for both directions; masked path: each valid direction into
+// prodm. Phi >= 1/2 for d >= 0.
+template <int P, bool TRUNC, bool MASKED>
+__device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double (&xj)[P], double dA, double dB,
+                                             bool vA, bool vB, double sqrt_tau, double (&racc)[P],
+                                             double (&cacc)[P], double& r2, double& prod, double& prodm) {
+    double dx[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) dx[q] = xi[q] - xj[q];
+    double d2 = dx[0] * dx[0];
+#pragma unroll
+    for (int q = 1; q < P; ++q) d2 = fma(dx[q], dx[q], d2);
+    if (MASKED && !(vA || vB)) return;
+    const double rs = rsqrt(d2);
+    const double d = d2 * rs;
+    const double resA = dA - d, resB = dB - d;
+    if (!MASKED || vA) r2 = fma(resA, resA, r2);
+    if (!MASKED || vB) r2 = fma(resB, resB, r2);
+    double t = 0.0;
+    if (TRUNC) {
+        const double z = d * sqrt_tau;
+        const double cdf = 0.5 * erfc(-z * 0.70710678118654752440);
+        const double pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
+        if (MASKED) {
+            if (vA) prodm *= cdf;
+            if (vB) prodm *= cdf;
+        } else {
+            prod *= cdf;
+        }
+        t = pdf * rs / (cdf * sqrt_tau);
+    }
+    if (!MASKED || vA) {
+        const double nc = fma(-resA, rs, t);
+#pragma unroll
+        for (int q = 0; q < P; ++q) racc[q] = fma(nc, dx[q], racc[q]);
+    }
+    if (!MASKED || vB) {
+        const double nc = fma(-resB, rs, t);
+#pragma unroll
+        for (int q = 0; q < P; ++q) cacc[q] = fma(nc, dx[q], cacc[q]);
+    }
+}
+
+// FP64 policy: scalar FP64 pairs over FP32-stored delta and FP64 locations;
+// FP64 partials; Phi multiplied into per-lane products, log taken every
+// kFoldUnits units.
+template <int P, bool TRUNC>
+struct PairMathF64 {
+    using X = double;
+    using Part = double;
+    static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
+    struct Cols {
+        double xj[4][P];
+        double acc[4][P];
+    };
+    struct Sums {
+        double r2, prod, l2, l1;  // l2: log of Phi products counted for both directions; l1: once
+        int since_fold;
+    };
+    double sqrt_tau;
+
+    __device__ explicit PairMathF64(const PairArgs& a) : sqrt_tau(a.sqrt_tau) {}
+
+    __device__ static void init(Sums& s) {
+        s.r2 = 0.0;
+        s.prod = 1.0;
+        s.l2 = s.l1 = 0.0;
+        s.since_fold = 0;
+    }
+    __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                cols.xj[c][q] = sXJ[q * kPairCols + lane + 32 * c];
+                cols.acc[c][q] = 0.0;
+            }
+    }
+    // One unit, row by row (one row's x_i and sums live at a time).
+    template <bool MASKED>
+    __device__ void unit(const float* sA, const float* sBl, const X* sXI, Cols& cols, Sums& s, int i0, int j0,
+                         int n, int lane, int warp, Part (&v)[4 * P]) const {
+        float4 b[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+        double prodm = 1.0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            double xi[P], racc[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                xi[q] = sXI[q * kPairRows + 4 * warp + r];
+                racc[q] = 0.0;
+            }
+            const int i = i0 + r;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int j = j0 + lane + 32 * c;
+                const float a = sA[(4 * warp + r) * kPairCols + lane + 32 * c];
+                const float bb = r == 0 ? b[c].x : r == 1 ? b[c].y : r == 2 ? b[c].z : b[c].w;
+                bool vA = true, vB = true;
+                if (MASKED) {
+                    const bool ok = (i < n) && (j < n) && (i > j);
+                    vA = ok && (a == a);
+                    vB = ok && (bb == bb);
+                }
+                pair_f64_sym<P, TRUNC, MASKED>(xi, cols.xj[c], (double)a, (double)bb, vA, vB, sqrt_tau, racc,
+                                               cols.acc[c], s.r2, s.prod, prodm);
+            }
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[r * P + q] = racc[q];
+        }
+        if (MASKED && TRUNC) s.l1 += log(prodm);  // <= 32 factors >= 1/2
+    }
+    __device__ static void after_unit(Sums& s) {
+        if (++s.since_fold == kFoldUnits) {
+            s.since_fold = 0;
+            if (TRUNC) {
+                s.l2 += log(s.prod);
+                s.prod = 1.0;
+            }
+        }
+    }
+    __device__ static Part col_value(const Cols& cols, int c, int q) { return cols.acc[c][q]; }
+    __device__ static void result(Sums& s, double& r2, double& lsum) {
+        r2 = s.r2;
+        lsum = TRUNC ? 2.0 * (s.l2 + log(s.prod)) + s.l1 : 0.0;
+    }
+};
+
 // --------------------------------------------------------------- the kernel
 
-template <int P, bool TRUNC>
+template <int P, bool TRUNC, class M>
 __global__ void __launch_bounds__(kPairThreads, 2)
     pair_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
                 const __grid_constant__ CUtensorMap tmap_xi, const __grid_constant__ CUtensorMap tmap_xj,
                 const PairArgs a) {
-    using Shape = PairShape<P>;
+    using X = typename M::X;
+    using Part = typename M::Part;
+    using Shape = PairShape<P, (int)sizeof(X)>;
+    constexpr int S = Shape::kStages;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                            ~uintptr_t(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + kPairStages * Shape::kStageBytes);
-    uint64_t* empty = full + kPairStages;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Shape::kStageBytes);
+    uint64_t* empty = full + S;
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
@@ -264,7 +482,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     const int J_first = pair_block_of_unit(u_begin, a.nb, a.nc);
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kPairStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], kPairWarps);
         }
@@ -284,17 +502,17 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     int pJ_loaded = -1;
     bool issue_ok = true;
     const uint64_t evict_first = l2_evict_first_policy();
-    // Issues units up to k + 2: unit m reuses the stage of unit m - kPairStages.
-    // The stage of m <= k + 1 was released before unit k - 1 began (bounded
-    // wait); the stage of k + 2 is taken only if already free, else it is
+    // Issues units up to k + S - 1: unit m reuses the stage of unit m - S. The
+    // stage of m <= k + S - 2 was released before unit k - 1 began (bounded
+    // wait); the stage of k + S - 1 is taken only if already free, else it is
     // issued before the next unit.
     auto top_up = [&](int k) {
-        while (issue_ok && issued < K && issued <= k + 2) {
+        while (issue_ok && issued < K && issued <= k + S - 1) {
             const int m = issued;
-            const int stage = m % kPairStages;
-            if (m >= kPairStages) {
-                const uint32_t par = ((uint32_t)(m / kPairStages) & 1u) ^ 1u;
-                if (m <= k + 1) {
+            const int stage = m % S;
+            if (m >= S) {
+                const uint32_t par = ((uint32_t)(m / S) & 1u) ^ 1u;
+                if (m <= k + S - 2) {
                     if (!mbar_wait_bounded(&empty[stage], par, a.err, kDevTimeoutEmpty)) {
                         issue_ok = false;
                         break;
@@ -322,18 +540,15 @@ __global__ void __launch_bounds__(kPairThreads, 2)
         }
     };
 
-    const PairConstsF32 kc{pk(-1.f, -1.f),         pk(a.k_e, a.k_e), pk(a.log2_k2, a.log2_k2),
-                           pk(-a.tp0, -a.tp0),     pk(-a.tp1, -a.tp1), pk(-a.tp2, -a.tp2),
-                           pk(a.ts0, a.ts0),       pk(a.ts1, a.ts1),   pk(a.ts2, a.ts2)};
+    const M math(a);
     // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
     // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
     const int b_off = lane * kPairRows + ((warp ^ (lane & 7)) << 2);
+    Part* rowpart = static_cast<Part*>(a.rowpart);
+    Part* colpart = static_cast<Part*>(a.colpart);
 
-    f2 r2 = pk(0.f, 0.f), prod = pk(1.f, 1.f);
-    // compensated FP32 sums (TwoSum): r^2, and log2 of 1/Phi products counted for both directions
-    float r2_hi = 0.f, r2_lo = 0.f, l2_hi = 0.f, l2_lo = 0.f;
-    float l1 = 0.f;  // log2 of masked-path products, counted once
-    int since_fold = 0;
+    typename M::Sums sums;
+    M::init(sums);
     bool alive = true;
     int k = 0;
     for (int J = J_first; k < K && alive; ++J) {
@@ -344,63 +559,39 @@ __global__ void __launch_bounds__(kPairThreads, 2)
         int I = 4 * J + (int)(u_begin + k - before);
         const int j0 = J * kPairCols;
 
-        f2 nxj[4][P];
-        f2 cacc[4][P];
-#pragma unroll
-        for (int c = 0; c < 4; ++c)
-#pragma unroll
-            for (int q = 0; q < P; ++q) cacc[c][q] = pk(0.f, 0.f);
+        typename M::Cols cols;
         bool j_masked = false;
 
         for (const int k_first = k; k < k_end; ++k, ++I) {
             if (issuer) top_up(k);
-            const int stage = k % kPairStages;
-            if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / kPairStages) & 1u, a.err, kDevTimeoutFull)) {
+            const int stage = k % S;
+            if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / S) & 1u, a.err, kDevTimeoutFull)) {
                 alive = false;
                 break;
             }
-            const float* st = reinterpret_cast<const float*>(smem + stage * Shape::kStageBytes);
-            const float* sB = st;
-            const float* sA = st + Shape::kBBytes / 4;
-            const float* sXI = st + Shape::kXIOffset / 4;
+            const unsigned char* st = smem + stage * Shape::kStageBytes;
+            const float* sB = reinterpret_cast<const float*>(st);
+            const float* sA = reinterpret_cast<const float*>(st + Shape::kBBytes);
+            const X* sXI = reinterpret_cast<const X*>(st + Shape::kXIOffset);
             if (k == k_first) {
-                // x_J arrived with this unit: negated (x_j, x_j) packs and the column flags
-                const float* sXJ = st + Shape::kXJOffset / 4;
+                // x_J arrived with this unit: the block's x_j and its column flags
+                const X* sXJ = reinterpret_cast<const X*>(st + Shape::kXJOffset);
+                M::begin_block(cols, sXJ, lane);
                 bool bad = false;
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-#pragma unroll
-                    for (int q = 0; q < P; ++q) {
-                        const float v = -sXJ[q * kPairCols + lane + 32 * c];
-                        nxj[c][q] = pk(v, v);
-                    }
-                    bad |= sXJ[P * kPairCols + lane + 32 * c] != 0.f;
-                }
+                for (int c = 0; c < 4; ++c) bad |= sXJ[P * kPairCols + lane + 32 * c] != X(0);
                 j_masked = __any_sync(0xffffffffu, bad);
             }
-            f2 xi[2][P];
-#pragma unroll
-            for (int q = 0; q < P; ++q) {
-                const float4 v = *reinterpret_cast<const float4*>(sXI + q * kPairRows + 4 * warp);
-                xi[0][q] = pk(v.x, v.y);
-                xi[1][q] = pk(v.z, v.w);
-            }
-            const float4 fl = *reinterpret_cast<const float4*>(sXI + P * kPairRows + 4 * warp);
+            const X* fl = sXI + P * kPairRows + 4 * warp;
             const bool masked =
-                j_masked || (I < 4 * J + 4) || fl.x != 0.f || fl.y != 0.f || fl.z != 0.f || fl.w != 0.f;
+                j_masked || (I < 4 * J + 4) || fl[0] != X(0) || fl[1] != X(0) || fl[2] != X(0) || fl[3] != X(0);
             const int i0 = I * kPairRows + 4 * warp;
 
-            f2 racc[2][P];
-#pragma unroll
-            for (int rp = 0; rp < 2; ++rp)
-#pragma unroll
-                for (int q = 0; q < P; ++q) racc[rp][q] = pk(0.f, 0.f);
+            Part v[4 * P];
             if (masked)
-                pair_unit<P, TRUNC, true>(sA, sB + b_off, xi, nxj, i0, j0, a.n, lane, warp, kc, racc, cacc, r2, prod,
-                                          l1);
+                math.template unit<true>(sA, sB + b_off, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
             else
-                pair_unit<P, TRUNC, false>(sA, sB + b_off, xi, nxj, i0, j0, a.n, lane, warp, kc, racc, cacc, r2,
-                                           prod, l1);
+                math.template unit<false>(sA, sB + b_off, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[stage]);
 
@@ -408,21 +599,12 @@ __global__ void __launch_bounds__(kPairThreads, 2)
             {
                 constexpr int KV = 4 * P;
                 using TS = TransposeShape<KV>;
-                float v[KV];
-#pragma unroll
-                for (int rp = 0; rp < 2; ++rp)
-#pragma unroll
-                    for (int q = 0; q < P; ++q) upk(racc[rp][q], v[(2 * rp) * P + q], v[(2 * rp + 1) * P + q]);
                 warp_transpose_reduce<KV>(v, lane);
                 const int idx = lane >> TS::kLaneShift;
                 if ((lane & ((1 << TS::kLaneShift) - 1)) == 0 && idx < KV)
-                    a.rowpart[((size_t)(u_begin + k) * kPairRows + 4 * warp) * P + idx] = v[0];
+                    rowpart[((size_t)(u_begin + k) * kPairRows + 4 * warp) * P + idx] = v[0];
             }
-
-            if (++since_fold == kPairFoldUnits) {
-                since_fold = 0;
-                fold_sums<TRUNC>(r2, prod, r2_hi, r2_lo, l2_hi, l2_lo);
-            }
+            M::after_unit(sums);
         }
         if (!alive) break;
         // column sums of block J from this CTA: [J][slot][warp][q][128]
@@ -430,22 +612,20 @@ __global__ void __launch_bounds__(kPairThreads, 2)
         for (int q = 0; q < P; ++q)
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-                a.colpart[(((size_t)J * a.max_slots + slot) * kPairWarps + warp) * (P * kPairCols) + q * kPairCols +
-                          lane + 32 * c] = sum2(cacc[c][q]);
+                colpart[(((size_t)J * a.max_slots + slot) * kPairWarps + warp) * (P * kPairCols) + q * kPairCols + lane +
+                        32 * c] = M::col_value(cols, c, q);
     }
 
     // The finish kernel may be scheduled now; it waits for this grid to complete.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (issuer) {
         // Copies still in flight (only after a failed wait): let them land before the CTA exits.
-        for (int m = k; m < issued; ++m)
-            mbar_wait_time_only(&full[m % kPairStages], (uint32_t)(m / kPairStages) & 1u);
+        for (int m = k; m < issued; ++m) mbar_wait_time_only(&full[m % S], (uint32_t)(m / S) & 1u);
     }
     if (!alive) return;
 
-    fold_sums<TRUNC>(r2, prod, r2_hi, r2_lo, l2_hi, l2_lo);
-    double r2_sum = (double)r2_hi + (double)r2_lo;
-    double lsum = -0.69314718055994530942 * (2.0 * ((double)l2_hi + (double)l2_lo) + (double)l1);
+    double r2_sum, lsum;
+    M::result(sums, r2_sum, lsum);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
@@ -453,26 +633,17 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     }
     if (lane == 0) {
         a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 0] = r2_sum;
-        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 1] = TRUNC ? lsum : 0.0;
+        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 1] = lsum;
     }
 }
 
-// Sums the partials of pair_kernel in a fixed order. Launched as a programmatic
-// dependent of the sweep: its blocks may be scheduled while the sweep drains and
-// wait (griddepcontrol.wait) until the sweep grid has completed and its writes
-// are visible. Block 0: the likelihood sums over CTAs and warps. Block nc - I:
-// the 32 rows of chunk I (32 P outputs), thread groups g = 0 .. kGroups-1 each
-// covering all outputs for the column blocks J = g, g + kGroups, ... of the row
-// sums and the slots of the column sums; every load of a chunk is issued before
-// it is summed (the partials are spread over the buffers: the kernel is bound by
-// load latency), and the groups combine in order g = 0, 1, ...
-// Sum of K floats (K a power of two) as a fixed pairwise tree: FP32 adds
-// only, as GB300 issues few FP64 operations per clock. Compile-time levels
-// keep the array in registers.
+// Sum of K values (K a power of two) as a fixed pairwise tree in their own
+// type: FP32 partials are added in FP32, as GB300 issues few FP64 operations
+// per clock. Compile-time levels keep the array in registers.
 template <int W>
 struct TreeLevel {
-    template <int K>
-    __device__ __forceinline__ static void fold(float (&v)[K]) {
+    template <typename T, int K>
+    __device__ __forceinline__ static void fold(T (&v)[K]) {
 #pragma unroll
         for (int k = 0; k < W; ++k) v[k] += v[k + W];
         TreeLevel<W / 2>::fold(v);
@@ -480,11 +651,11 @@ struct TreeLevel {
 };
 template <>
 struct TreeLevel<0> {
-    template <int K>
-    __device__ __forceinline__ static void fold(float (&)[K]) {}
+    template <typename T, int K>
+    __device__ __forceinline__ static void fold(T (&)[K]) {}
 };
-template <int K>
-__device__ __forceinline__ float tree_sum(float (&v)[K]) {
+template <int K, typename T>
+__device__ __forceinline__ T tree_sum(T (&v)[K]) {
     static_assert((K & (K - 1)) == 0, "K must be a power of two");
     TreeLevel<K / 2>::fold(v);
     return v[0];
@@ -498,9 +669,11 @@ struct FinishShape {
     static constexpr int kChunk = 8;                 // loads in flight per thread
 };
 
-template <int P>
+template <int P, typename Part>
 __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
     using FS = FinishShape<P>;
+    const Part* rowpart = static_cast<const Part*>(a.rowpart);
+    const Part* colpart = static_cast<const Part*>(a.colpart);
     asm volatile("griddepcontrol.wait;" ::: "memory");
     __shared__ double part[2][FS::kThreads];
     const int t = threadIdx.x;
@@ -548,12 +721,12 @@ __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
         // row sums: units (J, I), J = 0 .. I/4, each [32 rows][P] contiguous
         const int j_max = I >> 2;
         for (int J0 = g; J0 <= j_max; J0 += FS::kGroups * FS::kChunk) {
-            float v[FS::kChunk];
+            Part v[FS::kChunk];
 #pragma unroll
             for (int k = 0; k < FS::kChunk; ++k) {
                 const int J = J0 + FS::kGroups * k;
                 const long long u = pair_units_before(J, a.nc) + (I - 4 * J);
-                v[k] = J <= j_max ? __ldcg(&a.rowpart[(size_t)u * FS::kOut + o]) : 0.f;
+                v[k] = J <= j_max ? __ldcg(&rowpart[(size_t)u * FS::kOut + o]) : Part(0);
             }
             acc -= (double)tree_sum<FS::kChunk>(v);
         }
@@ -562,13 +735,13 @@ __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
         const long long before = pair_units_before(J, a.nc);
         const int n_e = a.j_slots[J] * kPairWarps;
         for (int e0 = g; e0 < n_e; e0 += FS::kGroups * 8) {
-            float v[8];
+            Part v[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int e = e0 + FS::kGroups * k;  // slot e / 8, warp e % 8
-                v[k] = e < n_e ? __ldcg(&a.colpart[((size_t)J * a.max_slots * kPairWarps + e) * (P * kPairCols) +
-                                                   q * kPairCols + jj])
-                               : 0.f;
+                v[k] = e < n_e ? __ldcg(&colpart[((size_t)J * a.max_slots * kPairWarps + e) * (P * kPairCols) +
+                                                 q * kPairCols + jj])
+                               : Part(0);
             }
             acc += (double)tree_sum<8>(v);
         }

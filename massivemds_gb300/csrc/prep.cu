@@ -69,10 +69,11 @@ __global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int n, long lo
     }
 }
 
+template <typename T>
 __global__ void write_flag_row_kernel(const int* __restrict__ row_nan, int n, int rows_padded,
-                                      float* __restrict__ flags, int x_ld) {
+                                      T* __restrict__ flags, int x_ld) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < x_ld; j += gridDim.x * blockDim.x)
-        flags[j] = (j >= n || (j < rows_padded && row_nan[j] != 0)) ? 1.0f : 0.0f;
+        flags[j] = (j >= n || (j < rows_padded && row_nan[j] != 0)) ? T(1) : T(0);
 }
 
 int grid_for(long long work, int threads) {
@@ -127,8 +128,14 @@ cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, i
     return cudaGetLastError();
 }
 
-cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, float* flags, int x_ld, cudaStream_t s) {
-    write_flag_row_kernel<<<grid_for(x_ld, 256), 256, 0, s>>>(row_nan, n, rows_padded, flags, x_ld);
+cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, void* flags, bool is_f32, int x_ld,
+                           cudaStream_t s) {
+    if (is_f32)
+        write_flag_row_kernel<float><<<grid_for(x_ld, 256), 256, 0, s>>>(row_nan, n, rows_padded,
+                                                                          static_cast<float*>(flags), x_ld);
+    else
+        write_flag_row_kernel<double><<<grid_for(x_ld, 256), 256, 0, s>>>(row_nan, n, rows_padded,
+                                                                           static_cast<double*>(flags), x_ld);
     return cudaGetLastError();
 }
 

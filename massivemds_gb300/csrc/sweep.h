@@ -55,12 +55,16 @@ struct PairMaps {
     CUtensorMap xi;  // locations + flag row, box 32 columns x (P + 1) rows
     CUtensorMap xj;  // the same, box 128 columns x (P + 1) rows
 };
+// FP32 mode and FP64 over FP32-stored delta, P <= kPairMaxP (f64: FP64 pair math and locations).
 bool pair_built(Mode mode, int p);
-cudaError_t pair_occupancy(int p, bool trunc, int* ctas_per_sm);
+cudaError_t pair_occupancy(int p, bool trunc, bool f64, int* ctas_per_sm);
 // Enqueues the pair sweep and its finish kernel (two launches).
-cudaError_t pair_launch(int p, bool trunc, const PairMaps& maps, const PairArgs& args, cudaStream_t stream);
-// flags[j] = 1 for j >= n or a NaN in row j of delta (row_nan), else 0, for j < x_ld.
-cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, float* flags, int x_ld, cudaStream_t s);
+cudaError_t pair_launch(int p, bool trunc, bool f64, const PairMaps& maps, const PairArgs& args,
+                        cudaStream_t stream);
+// flags[j] = 1 for j >= n or a NaN in row j of delta (row_nan), else 0, for j < x_ld,
+// in the location type (float or double).
+cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, void* flags, bool is_f32, int x_ld,
+                           cudaStream_t s);
 
 // Sets the message mdsx_last_error(NULL) returns on this thread (engine.cu).
 void set_global_error(const std::string& msg);

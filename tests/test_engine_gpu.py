@@ -7,7 +7,8 @@ Tolerances (from the engine's stated targets):
   FP32 mode (FP32 pairs, compensated FP32 partials, FP64 reductions): within
     1e-5 relative of the FP64 oracle on the same (FP32-rounded) delta, with
     either sweep schedule: "f32" is the engine's default (unordered pairs for
-    P <= 4 with truncation, else row blocks), "f32rows" and "f32pairs" force one.
+    P <= 4 with truncation, else row blocks), "f32rows" and "f32pairs" force one;
+    the same for FP64 over FP32-stored delta ("f64s32", "f64s32rows", "f64s32pairs").
 """
 import numpy as np
 import pytest
@@ -33,11 +34,12 @@ def grad_rel(g, ref):
 
 def make_engine(n, p, trunc, mode, delta, x, tau):
     fl = F.LEFT_TRUNCATION if trunc else 0
-    fl |= {"f64": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f32pairs": F.FLOAT, "f64s32": F.DELTA_F32}[mode]
+    fl |= {"f64": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f32pairs": F.FLOAT, "f64s32": F.DELTA_F32,
+           "f64s32rows": F.DELTA_F32, "f64s32pairs": F.DELTA_F32}[mode]
     e = Engine(p, n, fl)
-    if mode == "f32rows":
+    if mode.endswith("rows"):
         e.set_sweep_schedule(F.SWEEP_ROWS)
-    if mode == "f32pairs":
+    if mode.endswith("pairs"):
         e.set_sweep_schedule(F.SWEEP_PAIRS)
     e.setPairwiseData(delta)
     e.updateLocations(-1, x)
@@ -47,7 +49,7 @@ def make_engine(n, p, trunc, mode, delta, x, tau):
 
 
 def oracle_delta(delta, mode):
-    return delta.astype(np.float32) if mode in ("f32", "f32rows", "f32pairs", "f64s32") else delta
+    return delta.astype(np.float32) if mode != "f64" else delta
 
 
 def tolerances(mode):
@@ -123,7 +125,7 @@ def _inputs(n, p, seed, nans=0, asym=False):
     return delta, rng.standard_normal((n, p))
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32"])
+@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32rows", "f64s32pairs"])
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 31, 32, 33, 127, 128, 129, 159, 160, 161, 257, 385, 1000])
 def test_sizes_and_edges(mode, n):
     p, tau = 2, 1.7
@@ -143,10 +145,10 @@ def test_sizes_and_edges(mode, n):
         assert grad_rel(g, g_ref) < tol_g, trunc
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs"])
+@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32pairs"])
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_dimensions(mode, p):
-    if mode == "f32pairs" and p > 4:
+    if mode.endswith("pairs") and p > 4:
         pytest.skip("the unordered-pair schedule is built for P <= 4")
     n, tau = 300, 0.8
     delta, x = _inputs(n, p, seed=100 + p, nans=2, asym=True)
@@ -166,7 +168,7 @@ def test_nan_rows_and_asymmetric_delta():
     delta[5, :] = np.nan       # a whole row missing
     delta[:, 9] = np.nan       # a whole column missing
     delta[100, 101] = np.nan
-    for mode in ("f64", "f32rows", "f32pairs"):
+    for mode in ("f64", "f32rows", "f32pairs", "f64s32pairs"):
         tol_s, tol_g = tolerances(mode)
         e = make_engine(n, p, True, mode, delta, x, tau)
         s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -182,7 +184,7 @@ def test_precision_extremes():
     n, p = 500, 2
     delta, x = _inputs(n, p, seed=9)
     for tau in (1e-3, 0.05, 40.0, 900.0):
-        for mode in ("f64", "f32rows", "f32pairs"):
+        for mode in ("f64", "f32rows", "f32pairs", "f64s32pairs"):
             tol_s, tol_g = tolerances(mode)
             e = make_engine(n, p, True, mode, delta, x, tau)
             s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -239,7 +241,7 @@ def test_restore_returns_stored_sum_without_sweep():
 def test_deterministic_bitwise():
     n, p, tau = 3000, 2, 2.0
     delta, x = _inputs(n, p, seed=13)
-    for mode in ("f32rows", "f32pairs", "f64"):
+    for mode in ("f32rows", "f32pairs", "f64", "f64s32pairs"):
         e = make_engine(n, p, True, mode, delta, x, tau)
         s1, g1 = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
         e.makeDirty()
@@ -292,10 +294,11 @@ def test_error_statuses():
 
 
 def test_sweep_schedules():
-    """Truncated FP32 engines with P <= 4 default to the unordered-pair schedule
-    (sweep + finish kernel), untruncated ones to the row-block schedule; other
-    modes and dimensions run the row-block schedule and refuse the pair schedule;
-    switching invalidates the cached results."""
+    """Truncated engines with FP32-stored delta (FP32 or FP64 pair math) and
+    P <= 4 default to the unordered-pair schedule (sweep + finish kernel),
+    untruncated ones to the row-block schedule; FP64-stored delta and P > 4 run
+    the row-block schedule and refuse the pair schedule; switching invalidates
+    the cached results."""
     n, tau = 300, 1.3
     delta, x = _inputs(n, 2, seed=29)
     e = make_engine(n, 2, False, "f32", delta, x, tau)
@@ -304,7 +307,7 @@ def test_sweep_schedules():
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
     e.close()
     for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (5, "f32", F.SWEEP_ROWS),
-                             (2, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_ROWS)):
+                             (2, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_ROWS)):
         delta, x = _inputs(n, p, seed=30 + p)
         e = make_engine(n, p, True, mode, delta, x, tau)
         assert e.sweep_schedule() == default, (p, mode)
@@ -321,7 +324,8 @@ def test_sweep_schedules():
         s_rows = e.getSumOfIncrements()
         assert e.last_launch_count() == 1
         g_rows = e.getLogLikelihoodGradient()
-        assert rel(s_pairs, s_rows) < TOL_F32 and grad_rel(g_pairs, g_rows.reshape(n, p)) < TOL_F32
+        tol_s, tol_g = tolerances(mode if mode != "f64s32" else "f64")
+        assert rel(s_pairs, s_rows) < tol_s and grad_rel(g_pairs, g_rows.reshape(n, p)) < tol_g
         with pytest.raises(MdsxError):
             e.set_sweep_schedule(7)
         e.close()
@@ -340,13 +344,15 @@ def test_pair_schedule_symmetric_pairs_and_missing_blocks():
             delta[i, j] = np.nan  # (j, i) stays observed
         delta[n // 2, :] = np.nan
         for trunc in (True, False):
-            e = make_engine(n, p, trunc, "f32pairs", delta, x, tau)
-            assert e.sweep_schedule() == F.SWEEP_PAIRS
-            s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
-            e.close()
-            od = oracle_delta(delta, "f32")
-            assert rel(s, oracle.sum_of_increments(od, x, tau, trunc)) < TOL_F32, (n, trunc)
-            assert grad_rel(g, oracle.gradient(od, x, tau, trunc)) < TOL_F32, (n, trunc)
+            for mode in ("f32pairs", "f64s32pairs"):
+                e = make_engine(n, p, trunc, mode, delta, x, tau)
+                assert e.sweep_schedule() == F.SWEEP_PAIRS
+                s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+                e.close()
+                od = oracle_delta(delta, mode)
+                tol_s, tol_g = tolerances(mode)
+                assert rel(s, oracle.sum_of_increments(od, x, tau, trunc)) < tol_s, (n, trunc, mode)
+                assert grad_rel(g, oracle.gradient(od, x, tau, trunc)) < tol_g, (n, trunc, mode)
 
 
 # ------------------------------------------------------- device-resident API
@@ -383,7 +389,7 @@ def n20000():
     return delta, x, tau, oracle.sum_of_increments(delta, x, tau), oracle.gradient(delta, x, tau)
 
 
-@pytest.mark.parametrize("mode", ["f32rows", "f32pairs", "f64s32"])
+@pytest.mark.parametrize("mode", ["f32rows", "f32pairs", "f64s32rows", "f64s32pairs"])
 def test_full_size_n20000(mode, n20000):
     """The N=20 000, P=2, tau=2 workload with FP32-stored delta: one evaluation
     against the FP64 oracle on the same FP32 delta."""
