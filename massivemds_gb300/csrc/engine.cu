@@ -116,7 +116,7 @@ void free_all(mdsx_engine* e) {
 int plan_pairs(mdsx_engine* e) {
     int ctas = 0;
     const bool f64 = !e->x_f32;
-    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, f64, &ctas));
+    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, e->mode, &ctas));
     if (ctas < 1) return fail(e, MDSX_ECUDA, "pair sweep kernel cannot be resident on this device");
     e->pair_nb = (e->n + mdsx::kPairCols - 1) / mdsx::kPairCols;
     e->pair_nc = (e->n + mdsx::kPairRows - 1) / mdsx::kPairRows;
@@ -172,10 +172,11 @@ int plan_pairs(mdsx_engine* e) {
     MDSX_CUDA(e, cudaMalloc(&e->d_plpart, (size_t)e->pair_grid * mdsx::kPairWarps * 2 * sizeof(double)));
     for (int b = 0; b < 2; ++b) {
         mdsx::PairMaps& m = e->pair_maps[b];
-        int rc = make_tmap_2d(e, &m.a, e->d_delta, true, e->n, e->n, e->ld, mdsx::kPairCols, mdsx::kPairRows);
+        int rc = make_tmap_2d(e, &m.a, e->d_delta, e->delta_f32, e->n, e->n, e->ld, mdsx::kPairCols,
+                              mdsx::kPairRows);
         if (!rc)
-            rc = make_tmap_2d(e, &m.b, e->d_delta, true, e->n, e->n, e->ld, mdsx::kPairRows, mdsx::kPairCols,
-                              CU_TENSOR_MAP_SWIZZLE_128B);
+            rc = make_tmap_2d(e, &m.b, e->d_delta, e->delta_f32, e->n, e->n, e->ld, e->delta_f32 ? 32 : 16,
+                              mdsx::kPairCols, CU_TENSOR_MAP_SWIZZLE_128B);
         // the location maps span x_ld columns, so the flags of rows >= N are read from memory (1), not filled
         if (!rc)
             rc = make_tmap_2d(e, &m.xi, e->d_x[b], e->x_f32, e->x_ld, e->p + 1, e->x_ld, mdsx::kPairRows, e->p + 1);
@@ -343,7 +344,7 @@ int enqueue_sweep(mdsx_engine* e) {
         pa.grad_out = a.grad_out;
         pa.sums_out = a.sums_out;
         pa.err = a.err;
-        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, !e->x_f32, e->pair_maps[e->xcur], pa, e->stream));
+        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
         e->last_launches = 2;
         return MDSX_OK;
     }
@@ -674,8 +675,7 @@ int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
     if (schedule != MDSX_SWEEP_ROWS && schedule != MDSX_SWEEP_PAIRS)
         return fail(e, MDSX_EINVAL, "unknown sweep schedule");
     if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
-        return fail(e, MDSX_EUNSUPPORTED,
-                    "the unordered-pair schedule is built for FP32 and DELTA_F32 modes and P <= 4 only");
+        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for P <= 4 only");
     if (schedule != e->schedule) {
         e->schedule = schedule;
         e->sum_known = e->grad_known = false;

@@ -1,5 +1,6 @@
 // The fused sweep over unordered pairs: FP32 pair math (FP32 mode), or FP64
-// pair math over FP32-stored delta (DELTA_F32 mode), P <= kPairMaxP.
+// pair math over FP32-stored delta (DELTA_F32 mode) or FP64-stored delta
+// (default mode), P <= kPairMaxP.
 //
 // d_ij = d_ji, so everything a pair needs apart from delta -- the distance,
 // 1/d, Phi(d sqrt(tau)) and phi/Phi -- is computed once per unordered pair
@@ -17,8 +18,9 @@
 // contiguous range of units whose modelled cost is 1/G of the total (stream-K;
 // the host weights diagonal units and column-block starts, see
 // pair_unit_cost). Per unit the CTA loads with TMA
-//   A   = delta[I rows][J cols]   32 x 128 FP32, plain rows
-//   B   = delta[J rows][I cols]   128 x 32 FP32, 128-byte swizzled
+//   A   = delta[I rows][J cols]   32 x 128, plain rows
+//   B   = delta[J rows][I cols]   128 x 32, 128-byte swizzled (two boxes of 16
+//                                 columns for FP64 delta)
 //   x_I = P location rows + the flag row, 32 columns (compute type)
 //   x_J = the same over J's 128 columns, with the first unit of each J
 // into a ring of PairShape::kStages stages (mbarrier full/empty pairs). Lane 0
@@ -54,13 +56,17 @@ constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
 constexpr int kPairMaxP = 4;
 
-// XB: bytes per location element (4: FP32 math, 8: FP64 math). FP64 math is
-// bound by the FP64 pipe, so two stages hide the copies; FP32 math gets three.
-template <int P, int XB>
+// XB: bytes per location element (4: FP32 math, 8: FP64 math); SB: bytes per
+// delta element. FP64 math is bound by the FP64 pipe, so two stages hide the
+// copies; FP32 math gets three. B rows are 32 elements: with 8-byte delta they
+// come as two 128-byte-swizzled boxes of 16 columns (kBBoxes), one after the other.
+template <int P, int XB, int SB = 4>
 struct PairShape {
     static constexpr int kStages = XB == 4 ? 3 : 2;
-    static constexpr int kBBytes = kPairCols * kPairRows * 4;
-    static constexpr int kABytes = kPairRows * kPairCols * 4;
+    static constexpr int kBBoxCols = 128 / SB;
+    static constexpr int kBBoxes = kPairRows / kBBoxCols;
+    static constexpr int kBBytes = kPairCols * kPairRows * SB;
+    static constexpr int kABytes = kPairRows * kPairCols * SB;
     static constexpr int kXIBytes = (P + 1) * kPairRows * XB;
     static constexpr int kXJBytes = (P + 1) * kPairCols * XB;
     static constexpr int kXIOffset = kBBytes + kABytes;
@@ -252,6 +258,7 @@ __device__ __forceinline__ void fold_sums(f2& r2, f2& prod, float& r2_hi, float&
 template <int P, bool TRUNC>
 struct PairMathF32 {
     using X = float;     // location element in shared memory
+    using S = float;     // delta element
     using Part = float;  // row and column partials
     static constexpr int kFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
     struct Cols {        // one column block: negated (x_j, x_j) packs and the column sums
@@ -288,8 +295,11 @@ struct PairMathF32 {
     }
     // One unit: v[r * P + q] = this lane's sum of the (i, j) terms of row 4w + r.
     template <bool MASKED>
-    __device__ void unit(const float* sA, const float* sBl, const X* sXI, Cols& cols, Sums& s, int i0, int j0,
-                         int n, int lane, int warp, Part (&v)[4 * P]) const {
+    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
+                         int lane, int warp, Part (&v)[4 * P]) const {
+        // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
+        // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
+        const float* sBl = sB + lane * kPairRows + ((warp ^ (lane & 7)) << 2);
         f2 xi[2][P], racc[2][P];
 #pragma unroll
         for (int q = 0; q < P; ++q) {
@@ -323,7 +333,7 @@ struct PairMathF32 {
 // ------------------------------------------------------------ FP64 pair math
 
 // One unordered pair {i, j} in FP64 (CUDA double rsqrt, erfc, exp; one
-// division), both directions: dA = delta_ij, dB = delta_ji (FP32-stored).
+// division), both directions: dA = delta_ij, dB = delta_ji.
 // With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
 // -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
 // into cacc (signs as in the FP32 policy). Fast path: Phi multiplies into prod
@@ -370,12 +380,13 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
     }
 }
 
-// FP64 policy: scalar FP64 pairs over FP32-stored delta and FP64 locations;
+// FP64 policy: scalar FP64 pairs over FP32- or FP64-stored delta and FP64 locations;
 // FP64 partials; Phi multiplied into per-lane products, log taken every
 // kFoldUnits units.
-template <int P, bool TRUNC>
+template <int P, bool TRUNC, typename DeltaT>
 struct PairMathF64 {
     using X = double;
+    using S = DeltaT;  // float (DELTA_F32 mode) or double (FP64 mode)
     using Part = double;
     static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
@@ -405,13 +416,21 @@ struct PairMathF64 {
                 cols.acc[c][q] = 0.0;
             }
     }
+    // delta_ji for row 4w + r of the chunk and column j = lane + 32c of the block,
+    // from B's 128-byte-swizzled boxes of 128 / sizeof(S) columns.
+    __device__ static S b_value(const S* sB, int lane, int warp, int c, int r) {
+        constexpr int kBoxCols = 128 / (int)sizeof(S);     // 32 (float) or 16 (double)
+        constexpr int kChunkElems = 16 / (int)sizeof(S);   // 4 or 2
+        const int col = 4 * warp + r;                      // column of B = row of the chunk
+        const int box = col / kBoxCols, within = col - box * kBoxCols;
+        const int jj = lane + 32 * c;                      // row of B
+        const int chunk = (within / kChunkElems) ^ (jj & 7);
+        return sB[(box * kPairCols + jj) * kBoxCols + chunk * kChunkElems + within % kChunkElems];
+    }
     // One unit, row by row (one row's x_i and sums live at a time).
     template <bool MASKED>
-    __device__ void unit(const float* sA, const float* sBl, const X* sXI, Cols& cols, Sums& s, int i0, int j0,
-                         int n, int lane, int warp, Part (&v)[4 * P]) const {
-        float4 b[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) b[c] = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
+                         int lane, int warp, Part (&v)[4 * P]) const {
         double prodm = 1.0;
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
@@ -425,8 +444,8 @@ struct PairMathF64 {
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int j = j0 + lane + 32 * c;
-                const float a = sA[(4 * warp + r) * kPairCols + lane + 32 * c];
-                const float bb = r == 0 ? b[c].x : r == 1 ? b[c].y : r == 2 ? b[c].z : b[c].w;
+                const S a = sA[(4 * warp + r) * kPairCols + lane + 32 * c];
+                const S bb = b_value(sB, lane, warp, c, r);
                 bool vA = true, vB = true;
                 if (MASKED) {
                     const bool ok = (i < n) && (j < n) && (i > j);
@@ -465,8 +484,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
                 const __grid_constant__ CUtensorMap tmap_xi, const __grid_constant__ CUtensorMap tmap_xj,
                 const PairArgs a) {
     using X = typename M::X;
+    using DS = typename M::S;
     using Part = typename M::Part;
-    using Shape = PairShape<P, (int)sizeof(X)>;
+    using Shape = PairShape<P, (int)sizeof(X), (int)sizeof(DS)>;
     constexpr int S = Shape::kStages;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -527,7 +547,10 @@ __global__ void __launch_bounds__(kPairThreads, 2)
                 Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
             mbar_arrive_expect_tx(&full[stage], bytes);
             // delta is read once: evict it first, keeping the partials in L2 for the finish kernel
-            tma_load_2d_hint(st, &tmap_b, pI * kPairRows, pJ * kPairCols, &full[stage], evict_first);
+#pragma unroll
+            for (int bx = 0; bx < Shape::kBBoxes; ++bx)
+                tma_load_2d_hint(st + bx * (Shape::kBBytes / Shape::kBBoxes), &tmap_b,
+                                 pI * kPairRows + bx * Shape::kBBoxCols, pJ * kPairCols, &full[stage], evict_first);
             tma_load_2d_hint(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage], evict_first);
             tma_load_2d(st + Shape::kXIOffset, &tmap_xi, pI * kPairRows, 0, &full[stage]);
             if (new_j) tma_load_2d(st + Shape::kXJOffset, &tmap_xj, pJ * kPairCols, 0, &full[stage]);
@@ -541,9 +564,6 @@ __global__ void __launch_bounds__(kPairThreads, 2)
     };
 
     const M math(a);
-    // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
-    // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
-    const int b_off = lane * kPairRows + ((warp ^ (lane & 7)) << 2);
     Part* rowpart = static_cast<Part*>(a.rowpart);
     Part* colpart = static_cast<Part*>(a.colpart);
 
@@ -570,8 +590,8 @@ __global__ void __launch_bounds__(kPairThreads, 2)
                 break;
             }
             const unsigned char* st = smem + stage * Shape::kStageBytes;
-            const float* sB = reinterpret_cast<const float*>(st);
-            const float* sA = reinterpret_cast<const float*>(st + Shape::kBBytes);
+            const DS* sB = reinterpret_cast<const DS*>(st);
+            const DS* sA = reinterpret_cast<const DS*>(st + Shape::kBBytes);
             const X* sXI = reinterpret_cast<const X*>(st + Shape::kXIOffset);
             if (k == k_first) {
                 // x_J arrived with this unit: the block's x_j and its column flags
@@ -589,9 +609,9 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 
             Part v[4 * P];
             if (masked)
-                math.template unit<true>(sA, sB + b_off, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
+                math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
             else
-                math.template unit<false>(sA, sB + b_off, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
+                math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[stage]);
 

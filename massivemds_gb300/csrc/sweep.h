@@ -51,15 +51,15 @@ MDSX_DECLARE_MODE(f64s32)
 struct PairArgs;
 struct PairMaps {
     CUtensorMap a;   // delta, box 128 columns x 32 rows
-    CUtensorMap b;   // delta, box 32 columns x 128 rows, 128-byte swizzle
+    CUtensorMap b;   // delta, box 128 bytes (32 FP32 or 16 FP64 columns) x 128 rows, 128-byte swizzle
     CUtensorMap xi;  // locations + flag row, box 32 columns x (P + 1) rows
     CUtensorMap xj;  // the same, box 128 columns x (P + 1) rows
 };
-// FP32 mode and FP64 over FP32-stored delta, P <= kPairMaxP (f64: FP64 pair math and locations).
+// Built for every precision mode with P <= kPairMaxP.
 bool pair_built(Mode mode, int p);
-cudaError_t pair_occupancy(int p, bool trunc, bool f64, int* ctas_per_sm);
+cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm);
 // Enqueues the pair sweep and its finish kernel (two launches).
-cudaError_t pair_launch(int p, bool trunc, bool f64, const PairMaps& maps, const PairArgs& args,
+cudaError_t pair_launch(int p, bool trunc, Mode mode, const PairMaps& maps, const PairArgs& args,
                         cudaStream_t stream);
 // flags[j] = 1 for j >= n or a NaN in row j of delta (row_nan), else 0, for j < x_ld,
 // in the location type (float or double).

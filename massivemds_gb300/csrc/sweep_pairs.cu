@@ -1,6 +1,7 @@
 // Instances of the unordered-pair sweep (pair_kernel.cuh) -- FP32 pair math
-// (FP32 mode) and FP64 pair math over FP32-stored delta (DELTA_F32 mode), P = 1..kPairMaxP,
-// truncation on/off -- and the host-side launch of the sweep and its finish kernel.
+// (FP32 mode), FP64 pair math over FP32-stored delta (DELTA_F32 mode) and over
+// FP64-stored delta (default mode), P = 1..kPairMaxP, truncation on/off -- and
+// the host-side launch of the sweep and its finish kernel.
 #include <type_traits>
 
 #include "pair_kernel.cuh"
@@ -9,30 +10,36 @@
 namespace mdsx {
 namespace {
 
-template <int P, bool TRUNC, bool F64>
-using MathOf = typename std::conditional<F64, PairMathF64<P, TRUNC>, PairMathF32<P, TRUNC>>::type;
+// MODE: 0 FP32 math, 1 FP64 math over FP32 delta, 2 FP64 math over FP64 delta.
+template <int P, bool TRUNC, int MODE>
+using MathOf = typename std::conditional<
+    MODE == 0, PairMathF32<P, TRUNC>,
+    typename std::conditional<MODE == 1, PairMathF64<P, TRUNC, float>, PairMathF64<P, TRUNC, double>>::type>::type;
 
-template <int P, bool TRUNC, bool F64>
+template <int P, bool TRUNC, int MODE>
 constexpr int pair_smem_bytes() {
-    return PairShape<P, (int)sizeof(typename MathOf<P, TRUNC, F64>::X)>::kSmemBytes;
+    using M = MathOf<P, TRUNC, MODE>;
+    return PairShape<P, (int)sizeof(typename M::X), (int)sizeof(typename M::S)>::kSmemBytes;
 }
 
-template <int P, bool TRUNC, bool F64>
+int mode_index(Mode mode) { return mode == Mode::kF32 ? 0 : mode == Mode::kF64DeltaF32 ? 1 : 2; }
+
+template <int P, bool TRUNC, int MODE>
 cudaError_t pair_prepare() {
     static bool done = false;  // one engine thread at a time; idempotent if raced
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P, TRUNC, MathOf<P, TRUNC, F64>>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, pair_smem_bytes<P, TRUNC, F64>());
+    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P, TRUNC, MathOf<P, TRUNC, MODE>>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, pair_smem_bytes<P, TRUNC, MODE>());
     if (e == cudaSuccess) done = true;
     return e;
 }
 
-template <int P, bool TRUNC, bool F64>
+template <int P, bool TRUNC, int MODE>
 cudaError_t pair_launch_one(const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
-    using M = MathOf<P, TRUNC, F64>;
-    cudaError_t e = pair_prepare<P, TRUNC, F64>();
+    using M = MathOf<P, TRUNC, MODE>;
+    cudaError_t e = pair_prepare<P, TRUNC, MODE>();
     if (e != cudaSuccess) return e;
-    pair_kernel<P, TRUNC, M><<<args.grid, kPairThreads, pair_smem_bytes<P, TRUNC, F64>(), stream>>>(
+    pair_kernel<P, TRUNC, M><<<args.grid, kPairThreads, pair_smem_bytes<P, TRUNC, MODE>(), stream>>>(
         maps.a, maps.b, maps.xi, maps.xj, args);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -51,52 +58,66 @@ cudaError_t pair_launch_one(const PairMaps& maps, const PairArgs& args, cudaStre
     return cudaLaunchKernelEx(&cfg, pair_finish_kernel<P, typename M::Part>, args);
 }
 
-template <int P, bool TRUNC, bool F64>
+template <int P, bool TRUNC, int MODE>
 cudaError_t pair_occupancy_one(int* ctas) {
-    cudaError_t e = pair_prepare<P, TRUNC, F64>();
+    cudaError_t e = pair_prepare<P, TRUNC, MODE>();
     if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, pair_kernel<P, TRUNC, MathOf<P, TRUNC, F64>>,
-                                                         kPairThreads, pair_smem_bytes<P, TRUNC, F64>());
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, pair_kernel<P, TRUNC, MathOf<P, TRUNC, MODE>>,
+                                                         kPairThreads, pair_smem_bytes<P, TRUNC, MODE>());
+}
+
+template <int P, int MODE>
+cudaError_t pair_launch_pm(bool trunc, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
+    return trunc ? pair_launch_one<P, true, MODE>(maps, args, stream)
+                 : pair_launch_one<P, false, MODE>(maps, args, stream);
 }
 
 template <int P>
-cudaError_t pair_launch_p(bool trunc, bool f64, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
-    if (f64)
-        return trunc ? pair_launch_one<P, true, true>(maps, args, stream)
-                     : pair_launch_one<P, false, true>(maps, args, stream);
-    return trunc ? pair_launch_one<P, true, false>(maps, args, stream)
-                 : pair_launch_one<P, false, false>(maps, args, stream);
+cudaError_t pair_launch_p(bool trunc, int mode, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
+    switch (mode) {
+        case 0: return pair_launch_pm<P, 0>(trunc, maps, args, stream);
+        case 1: return pair_launch_pm<P, 1>(trunc, maps, args, stream);
+        default: return pair_launch_pm<P, 2>(trunc, maps, args, stream);
+    }
+}
+
+template <int P, int MODE>
+cudaError_t pair_occupancy_pm(bool trunc, int* ctas) {
+    return trunc ? pair_occupancy_one<P, true, MODE>(ctas) : pair_occupancy_one<P, false, MODE>(ctas);
 }
 
 template <int P>
-cudaError_t pair_occupancy_p(bool trunc, bool f64, int* ctas) {
-    if (f64) return trunc ? pair_occupancy_one<P, true, true>(ctas) : pair_occupancy_one<P, false, true>(ctas);
-    return trunc ? pair_occupancy_one<P, true, false>(ctas) : pair_occupancy_one<P, false, false>(ctas);
+cudaError_t pair_occupancy_p(bool trunc, int mode, int* ctas) {
+    switch (mode) {
+        case 0: return pair_occupancy_pm<P, 0>(trunc, ctas);
+        case 1: return pair_occupancy_pm<P, 1>(trunc, ctas);
+        default: return pair_occupancy_pm<P, 2>(trunc, ctas);
+    }
 }
 
 }  // namespace
 
-bool pair_built(Mode mode, int p) {
-    return (mode == Mode::kF32 || mode == Mode::kF64DeltaF32) && p >= 1 && p <= kPairMaxP;
-}
+bool pair_built(Mode, int p) { return p >= 1 && p <= kPairMaxP; }
 
-cudaError_t pair_occupancy(int p, bool trunc, bool f64, int* ctas_per_sm) {
+cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm) {
+    const int m = mode_index(mode);
     switch (p) {
-        case 1: return pair_occupancy_p<1>(trunc, f64, ctas_per_sm);
-        case 2: return pair_occupancy_p<2>(trunc, f64, ctas_per_sm);
-        case 3: return pair_occupancy_p<3>(trunc, f64, ctas_per_sm);
-        case 4: return pair_occupancy_p<4>(trunc, f64, ctas_per_sm);
+        case 1: return pair_occupancy_p<1>(trunc, m, ctas_per_sm);
+        case 2: return pair_occupancy_p<2>(trunc, m, ctas_per_sm);
+        case 3: return pair_occupancy_p<3>(trunc, m, ctas_per_sm);
+        case 4: return pair_occupancy_p<4>(trunc, m, ctas_per_sm);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t pair_launch(int p, bool trunc, bool f64, const PairMaps& maps, const PairArgs& args,
+cudaError_t pair_launch(int p, bool trunc, Mode mode, const PairMaps& maps, const PairArgs& args,
                         cudaStream_t stream) {
+    const int m = mode_index(mode);
     switch (p) {
-        case 1: return pair_launch_p<1>(trunc, f64, maps, args, stream);
-        case 2: return pair_launch_p<2>(trunc, f64, maps, args, stream);
-        case 3: return pair_launch_p<3>(trunc, f64, maps, args, stream);
-        case 4: return pair_launch_p<4>(trunc, f64, maps, args, stream);
+        case 1: return pair_launch_p<1>(trunc, m, maps, args, stream);
+        case 2: return pair_launch_p<2>(trunc, m, maps, args, stream);
+        case 3: return pair_launch_p<3>(trunc, m, maps, args, stream);
+        case 4: return pair_launch_p<4>(trunc, m, maps, args, stream);
         default: return cudaErrorInvalidValue;
     }
 }

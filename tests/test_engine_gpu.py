@@ -8,7 +8,8 @@ Tolerances (from the engine's stated targets):
     1e-5 relative of the FP64 oracle on the same (FP32-rounded) delta, with
     either sweep schedule: "f32" is the engine's default (unordered pairs for
     P <= 4 with truncation, else row blocks), "f32rows" and "f32pairs" force one;
-    the same for FP64 over FP32-stored delta ("f64s32", "f64s32rows", "f64s32pairs").
+    the same for FP64 over FP32-stored delta ("f64s32", "f64s32rows", "f64s32pairs")
+    and over FP64-stored delta ("f64", "f64rows", "f64pairs").
 """
 import numpy as np
 import pytest
@@ -34,8 +35,8 @@ def grad_rel(g, ref):
 
 def make_engine(n, p, trunc, mode, delta, x, tau):
     fl = F.LEFT_TRUNCATION if trunc else 0
-    fl |= {"f64": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f32pairs": F.FLOAT, "f64s32": F.DELTA_F32,
-           "f64s32rows": F.DELTA_F32, "f64s32pairs": F.DELTA_F32}[mode]
+    fl |= {"f64": 0, "f64rows": 0, "f64pairs": 0, "f32": F.FLOAT, "f32rows": F.FLOAT, "f32pairs": F.FLOAT,
+           "f64s32": F.DELTA_F32, "f64s32rows": F.DELTA_F32, "f64s32pairs": F.DELTA_F32}[mode]
     e = Engine(p, n, fl)
     if mode.endswith("rows"):
         e.set_sweep_schedule(F.SWEEP_ROWS)
@@ -49,7 +50,7 @@ def make_engine(n, p, trunc, mode, delta, x, tau):
 
 
 def oracle_delta(delta, mode):
-    return delta.astype(np.float32) if mode != "f64" else delta
+    return delta if mode.startswith("f64") and not mode.startswith("f64s32") else delta.astype(np.float32)
 
 
 def tolerances(mode):
@@ -58,14 +59,17 @@ def tolerances(mode):
 
 # ------------------------------------------------------------- golden vectors
 
-def test_fp64_matches_reference_golden(golden):
+@pytest.mark.parametrize("mode", ["f64rows", "f64pairs"])
+def test_fp64_matches_reference_golden(golden, mode):
     data, cases = golden
     for name in cases:
         n, p, trunc, tau, use_float = data[f"{name}.meta"]
         if use_float:
             continue
         n, p = int(n), int(p)
-        e = make_engine(n, p, bool(trunc), "f64", data[f"{name}.delta"], data[f"{name}.x"], tau)
+        if mode == "f64pairs" and p > 4:
+            continue
+        e = make_engine(n, p, bool(trunc), mode, data[f"{name}.delta"], data[f"{name}.x"], tau)
         s = e.getSumOfIncrements()
         g = e.getLogLikelihoodGradient()
         e.close()
@@ -94,7 +98,7 @@ def test_reference_call_sequence_golden(golden):
     data, _ = golden
     delta, x0, tau = data["seq.delta"], data["seq.x0"], float(data["seq.tau"])
     n, p = x0.shape
-    for mode in ("f64", "f32"):
+    for mode in ("f64rows", "f64pairs", "f32rows", "f32pairs"):
         tol_s, tol_g = tolerances(mode)
         e = make_engine(n, p, True, mode, delta, x0, tau)
         assert rel(e.getSumOfIncrements(), data["seq.sums"][0]) < tol_s
@@ -125,7 +129,7 @@ def _inputs(n, p, seed, nans=0, asym=False):
     return delta, rng.standard_normal((n, p))
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32rows", "f64s32pairs"])
+@pytest.mark.parametrize("mode", ["f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32rows", "f64s32pairs"])
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 31, 32, 33, 127, 128, 129, 159, 160, 161, 257, 385, 1000])
 def test_sizes_and_edges(mode, n):
     p, tau = 2, 1.7
@@ -145,7 +149,7 @@ def test_sizes_and_edges(mode, n):
         assert grad_rel(g, g_ref) < tol_g, trunc
 
 
-@pytest.mark.parametrize("mode", ["f64", "f32rows", "f32pairs", "f64s32pairs"])
+@pytest.mark.parametrize("mode", ["f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32pairs"])
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_dimensions(mode, p):
     if mode.endswith("pairs") and p > 4:
@@ -168,7 +172,7 @@ def test_nan_rows_and_asymmetric_delta():
     delta[5, :] = np.nan       # a whole row missing
     delta[:, 9] = np.nan       # a whole column missing
     delta[100, 101] = np.nan
-    for mode in ("f64", "f32rows", "f32pairs", "f64s32pairs"):
+    for mode in ("f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32pairs"):
         tol_s, tol_g = tolerances(mode)
         e = make_engine(n, p, True, mode, delta, x, tau)
         s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -184,7 +188,7 @@ def test_precision_extremes():
     n, p = 500, 2
     delta, x = _inputs(n, p, seed=9)
     for tau in (1e-3, 0.05, 40.0, 900.0):
-        for mode in ("f64", "f32rows", "f32pairs", "f64s32pairs"):
+        for mode in ("f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32pairs"):
             tol_s, tol_g = tolerances(mode)
             e = make_engine(n, p, True, mode, delta, x, tau)
             s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -241,7 +245,7 @@ def test_restore_returns_stored_sum_without_sweep():
 def test_deterministic_bitwise():
     n, p, tau = 3000, 2, 2.0
     delta, x = _inputs(n, p, seed=13)
-    for mode in ("f32rows", "f32pairs", "f64", "f64s32pairs"):
+    for mode in ("f32rows", "f32pairs", "f64rows", "f64pairs", "f64s32pairs"):
         e = make_engine(n, p, True, mode, delta, x, tau)
         s1, g1 = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
         e.makeDirty()
@@ -294,11 +298,10 @@ def test_error_statuses():
 
 
 def test_sweep_schedules():
-    """Truncated engines with FP32-stored delta (FP32 or FP64 pair math) and
-    P <= 4 default to the unordered-pair schedule (sweep + finish kernel),
-    untruncated ones to the row-block schedule; FP64-stored delta and P > 4 run
-    the row-block schedule and refuse the pair schedule; switching invalidates
-    the cached results."""
+    """Truncated engines with P <= 4 (every precision mode) default to the
+    unordered-pair schedule (sweep + finish kernel), untruncated ones to the
+    row-block schedule; P > 4 runs the row-block schedule and refuses the pair
+    schedule; switching invalidates the cached results."""
     n, tau = 300, 1.3
     delta, x = _inputs(n, 2, seed=29)
     e = make_engine(n, 2, False, "f32", delta, x, tau)
@@ -307,7 +310,8 @@ def test_sweep_schedules():
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
     e.close()
     for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (5, "f32", F.SWEEP_ROWS),
-                             (2, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_ROWS)):
+                             (2, "f64", F.SWEEP_PAIRS), (5, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS),
+                             (5, "f64s32", F.SWEEP_ROWS)):
         delta, x = _inputs(n, p, seed=30 + p)
         e = make_engine(n, p, True, mode, delta, x, tau)
         assert e.sweep_schedule() == default, (p, mode)
@@ -324,7 +328,7 @@ def test_sweep_schedules():
         s_rows = e.getSumOfIncrements()
         assert e.last_launch_count() == 1
         g_rows = e.getLogLikelihoodGradient()
-        tol_s, tol_g = tolerances(mode if mode != "f64s32" else "f64")
+        tol_s, tol_g = tolerances(mode)
         assert rel(s_pairs, s_rows) < tol_s and grad_rel(g_pairs, g_rows.reshape(n, p)) < tol_g
         with pytest.raises(MdsxError):
             e.set_sweep_schedule(7)
@@ -344,7 +348,7 @@ def test_pair_schedule_symmetric_pairs_and_missing_blocks():
             delta[i, j] = np.nan  # (j, i) stays observed
         delta[n // 2, :] = np.nan
         for trunc in (True, False):
-            for mode in ("f32pairs", "f64s32pairs"):
+            for mode in ("f32pairs", "f64s32pairs", "f64pairs"):
                 e = make_engine(n, p, trunc, mode, delta, x, tau)
                 assert e.sweep_schedule() == F.SWEEP_PAIRS
                 s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
@@ -361,7 +365,7 @@ def test_device_api_matches_host_api():
     torch = pytest.importorskip("torch")
     n, p, tau = 700, 2, 2.0
     delta, x = _inputs(n, p, seed=16)
-    for mode in ("f32rows", "f32pairs", "f64"):
+    for mode in ("f32rows", "f32pairs", "f64rows", "f64pairs"):
         e = make_engine(n, p, True, mode, delta, x, tau)
         s_host, g_host = e.getSumOfIncrements(), e.getLogLikelihoodGradient().copy()
         dx = torch.tensor(x, dtype=torch.float64, device="cuda")
