@@ -43,9 +43,10 @@ N, P, TAU = 20000, 2, 2.0
 EVALS_PER_STEP = 200
 METRIC = "loglik+grad evals/s & HBM GB/s at N=20k; HMC minESS/s surrogate vs plain, 1 GPU"
 UNIT = "evals/s"
-def workload(n: int) -> str:
+def workload(n: int, precision: str = "f32", evals: int = EVALS_PER_STEP) -> str:
+    math = "FP32 pairs + FP64 reductions" if precision == "f32" else "FP64 pairs (DELTA_F32 mode)"
     return (f"fused loglik+grad sweep, N={n}, P=2, tau=2, truncation, delta FP32-stored ({n * n * 4 / 1e9:.2f} GB), "
-            "FP32 pairs + FP64 reductions, 200 evals per step at fresh locations")
+            f"{math}, {evals} evals per step at fresh locations")
 DATA = ("synthetic: delta = ||Y_i - Y_j|| + N(0, 0.05^2) noise clipped at 0, Y ~ N(0, I_10) (seed 666); "
         "x ~ N(0,1) per evaluation")
 
@@ -57,6 +58,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mdsx", choices=["mdsx", "reference"])
     ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"],
+                    help="pair arithmetic: f32 (the headline; FP32 pairs, FP64 reductions) or f64 (FP64 pairs over "
+                         "the same FP32-stored delta; bound by the FP64 pipe, 10 evaluations per step)")
     ap.add_argument("--schedule", default="pairs", choices=["pairs", "rows"],
                     help="sweep schedule: each unordered pair once (default) or the row-block schedule")
     ap.add_argument("--cpu-seconds", type=float, default=4.0, help="wall time of one CPU baseline sample")
@@ -312,8 +316,10 @@ def run_mdsx(args):
     import massivemds_gb300 as m
 
     n = args.n
+    f64 = args.precision == "f64"
+    evals = 10 if f64 else EVALS_PER_STEP
     delta = make_delta(n)
-    eng = m.Engine(P, n, m.flags.FLOAT | m.flags.LEFT_TRUNCATION, local)
+    eng = m.Engine(P, n, (m.flags.DELTA_F32 if f64 else m.flags.FLOAT) | m.flags.LEFT_TRUNCATION, local)
     eng.set_sweep_schedule(m.flags.SWEEP_PAIRS if args.schedule == "pairs" else m.flags.SWEEP_ROWS)
     eng.setPairwiseData(delta)
     eng.setParameters([TAU])
@@ -322,12 +328,12 @@ def run_mdsx(args):
 
     # location pool: one set per evaluation of a step
     rng = np.random.default_rng(1000 + rank)
-    pool_host = torch.from_numpy(rng.standard_normal((EVALS_PER_STEP, n, P))).pin_memory()
+    pool_host = torch.from_numpy(rng.standard_normal((evals, n, P))).pin_memory()
     pool_dev = pool_host.to(f"cuda:{local}")
     d_sum = torch.zeros(1, dtype=torch.float64, device=f"cuda:{local}")
 
     def device_step(events=None):
-        for k in range(EVALS_PER_STEP):
+        for k in range(evals):
             eng.update_locations_device(pool_dev[k].data_ptr())
             if events is not None:
                 events[k][0].record(stream)
@@ -344,7 +350,7 @@ def run_mdsx(args):
     sampler.start()
     time.sleep(0.5)
     kev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-            for _ in range(EVALS_PER_STEP)] for _ in range(args.steps)]
+            for _ in range(evals)] for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         torch.distributed.barrier()
@@ -362,17 +368,17 @@ def run_mdsx(args):
     elapsed_ms = start.elapsed_time(stop)
     kernel_ms = statistics.mean(a.elapsed_time(b) for ev in kev for a, b in ev)
     launches = eng.last_launch_count()  # sweep launches per evaluation
-    gpu_launches = args.steps * EVALS_PER_STEP * (launches + 1)  # + the location conversion kernel
+    gpu_launches = args.steps * evals * (launches + 1)  # + the location conversion kernel
 
     elapsed_ms = across_ranks_max(elapsed_ms, world, f"cuda:{local}")
-    value = job_throughput(args.steps * EVALS_PER_STEP, world, elapsed_ms / 1000.0)
+    value = job_throughput(args.steps * evals, world, elapsed_ms / 1000.0)
 
     # end to end through the reference-facing API with host buffers
     eng.set_stream(None)
     grad_host = torch.empty(n * P, dtype=torch.float64).pin_memory()
     g_np = grad_host.numpy()
     pool_np = pool_host.numpy()
-    for k in range(min(EVALS_PER_STEP, 10)):
+    for k in range(min(evals, 10)):
         eng.updateLocations(-1, pool_np[k])
         eng.getSumOfIncrements()
         eng.getLogLikelihoodGradient(g_np)
@@ -381,20 +387,25 @@ def run_mdsx(args):
         torch.distributed.barrier()
     t = time.perf_counter()
     for _ in range(e2e_steps):
-        for k in range(EVALS_PER_STEP):
+        for k in range(evals):
             eng.updateLocations(-1, pool_np[k])
             eng.getSumOfIncrements()
             eng.getLogLikelihoodGradient(g_np)
     e2e_s = time.perf_counter() - t
     e2e_s = across_ranks_max(e2e_s, world, f"cuda:{local}")
-    e2e_value = job_throughput(e2e_steps * EVALS_PER_STEP, world, e2e_s)
+    e2e_value = job_throughput(e2e_steps * evals, world, e2e_s)
 
     hbm_peak, peak_kind = peaks()
     bytes_per_launch = float(n) * n * 4 + 2.0 * n * P * 4
     achieved = bytes_per_launch / (kernel_ms / 1000.0) / 1e9
     traffic = profiled_traffic(args.schedule) if n == N else None  # the committed captures are of N = 20000
-    kernel_name = ("pair_kernel<2,true> + pair_finish_kernel<2>" if args.schedule == "pairs"
-                   else "sweep_kernel<float,float,2,true>")
+    if f64:
+        kernel_name = ("pair_kernel<2,true,PairMathF64<float>> + pair_finish_kernel<2,double>"
+                       if args.schedule == "pairs" else "sweep_kernel<double,float,2,true>")
+        traffic = None  # FP64-pipe bound: the HBM fraction below is small by construction
+    else:
+        kernel_name = ("pair_kernel<2,true,PairMathF32> + pair_finish_kernel<2,float>" if args.schedule == "pairs"
+                       else "sweep_kernel<float,float,2,true>")
 
     line = None
     if rank == 0:
@@ -403,9 +414,9 @@ def run_mdsx(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
-            "config": {"workload": workload(n), "n": n, "p": P, "tau": TAU, "evals_per_step": EVALS_PER_STEP,
-                       "schedule": args.schedule,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision, "data": DATA,
+            "config": {"workload": workload(n, args.precision, evals), "n": n, "p": P, "tau": TAU, "evals_per_step": evals,
+                       "schedule": args.schedule, "precision": args.precision,
                        "delta_bytes": n * n * 4, "l2": f"inputs larger than L2 ({n * n * 4 / 1e9:.2f} GB delta vs 129 MB L2), no flush",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
@@ -413,8 +424,8 @@ def run_mdsx(args):
                          "kernel": kernel_name, "kernel_ms": kernel_ms,
                          "peak_kind": peak_kind},
             "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": EVALS_PER_STEP * n * P * 8,
-                    "d2h_bytes_per_step": EVALS_PER_STEP * (n * P * 8 + 32)},
+                    "h2d_bytes_per_step": evals * n * P * 8,
+                    "d2h_bytes_per_step": evals * (n * P * 8 + 32)},
             "gpu_launches": gpu_launches,
             "clocks": sampler.summary(t0, t1),
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
