@@ -124,12 +124,14 @@ class Batch:
 
     def group_shape(self, p: int) -> tuple[int, int, int, int]:
         """(schedule, rows per warp, CTAs per SM, grid) of dimension p's group;
-        schedule 0 = stream-K units, 1 = row-block queue."""
+        schedule 0 = stream-K units, 1 = row-block queue, 2 = unordered pairs."""
         sc, rw, ctas, grid = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._check(self._lib.mdsx_batch_group_shape(self._h, int(p), ctypes.byref(sc), ctypes.byref(rw),
                                                      ctypes.byref(ctas), ctypes.byref(grid)))
         return sc.value, rw.value, ctas.value, grid.value
 
     def force_shape(self, p: int, rows_per_warp: int, ctas_per_sm: int = 2, schedule: int = 1) -> None:
+        """Fixes dimension p's shape (schedule 2 needs P <= 4 and rows_per_warp 4);
+        rows_per_warp 0 removes the override."""
         self._check(self._lib.mdsx_batch_force_shape(self._h, int(p), int(schedule), int(rows_per_warp),
                                                      int(ctas_per_sm)))

@@ -159,7 +159,7 @@ def main(argv=None):
         "speedup_vs_engines": t_engines / t_batch,
         "speedup_vs_engines_sync": t_sync / t_batch,
         "tuned_candidates": candidates,
-        "shapes": {str(p): {"schedule": ("stream-K", "row-block queue")[s[0]], "rows_per_warp": s[1],
+        "shapes": {str(p): {"schedule": ("stream-K", "row-block queue", "unordered pairs")[s[0]], "rows_per_warp": s[1],
                             "ctas_per_sm": s[2], "grid": s[3]} for p, s in shapes.items()},
         "setup_seconds": setup_s,
     }

@@ -7,9 +7,11 @@
 // setPairwiseData, setParameters, makeDirty), by one object that owns every
 // instance's data on one GPU and evaluates all of them with one persistent
 // launch per (P, truncation) group, the launches captured once as a CUDA
-// graph. Two schedules: stream-K over (row block x 128 columns) units of all
-// instances (batch_kernel.cuh), and a queue of whole row blocks taken
-// dynamically, largest instance first (batch_queue.cuh). Results of all instances come back in one
+// graph. Three schedules: stream-K over (row block x 128 columns) units of all
+// instances (batch_kernel.cuh), a queue of whole row blocks taken
+// dynamically, largest instance first (batch_queue.cuh), and stream-K over the
+// unordered-pair units of all instances with a finish kernel (batch_pairs.cuh,
+// P <= 4). Results of all instances come back in one
 // device-to-host copy. Instance calls keep the reference's names and lazy
 // semantics: a getter evaluates the batch when any instance changed.
 //
@@ -152,6 +154,11 @@ struct BatchInst {
     unsigned* d_counts = nullptr;  // [R] row-block counters + [1] done counter
     double* d_qlpart = nullptr;    // queue schedule: [R][warps][2] likelihood partials
     unsigned* d_qdone = nullptr;   // queue schedule: row blocks finished
+    float* d_prow = nullptr;       // pair schedule: row partials [units][32][P]
+    float* d_pcol = nullptr;       // pair schedule: column partials [nb][max_slots][8][P][128]
+    double* d_plp = nullptr;       // pair schedule: likelihood partials [CTAs meeting it][8][2]
+    int* d_pjfirst = nullptr;      // pair schedule: first CTA per column block
+    int* d_pjslots = nullptr;      // pair schedule: CTAs per column block
     long long grad_off = 0;        // offset (doubles) in the concatenated gradients
 };
 
@@ -174,6 +181,11 @@ struct BatchGroup {
     mdsx::batch::QueueInstance* d_qdesc = nullptr;
     unsigned long long* d_next = nullptr;
     long long n_items = 0;
+    // unordered-pair schedule
+    std::vector<mdsx::batch::PairInstance> h_pdesc;  // in member order
+    mdsx::batch::PairInstance* d_pdesc = nullptr;
+    long long* d_pbegin = nullptr;  // [grid + 1] global units per CTA
+    int finish_blocks = 0;
     double work = 0.0;  // modelled cost: sum of N^2 x (16 + 3P) instructions per pair
 };
 
@@ -231,6 +243,14 @@ struct Guard {
 };
 
 void free_plan_scratch(BatchInst& in) {
+    cudaFree(in.d_prow);
+    cudaFree(in.d_pcol);
+    cudaFree(in.d_plp);
+    cudaFree(in.d_pjfirst);
+    cudaFree(in.d_pjslots);
+    in.d_prow = in.d_pcol = nullptr;
+    in.d_plp = nullptr;
+    in.d_pjfirst = in.d_pjslots = nullptr;
     cudaFree(in.d_qlpart);
     cudaFree(in.d_qdone);
     in.d_qlpart = nullptr;
@@ -261,6 +281,8 @@ void free_plan(mdsx_batch* b) {
         cudaFree(g.d_desc);
         cudaFree(g.d_qdesc);
         cudaFree(g.d_next);
+        cudaFree(g.d_pdesc);
+        cudaFree(g.d_pbegin);
     }
     b->groups.clear();
     for (auto& in : b->inst) free_plan_scratch(in);
@@ -274,7 +296,7 @@ void free_plan(mdsx_batch* b) {
 }
 
 int make_tmap(mdsx_batch* b, CUtensorMap* map, void* base, long long cols, long long rows, long long ld,
-              unsigned box_cols, unsigned box_rows) {
+              unsigned box_cols, unsigned box_rows, CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE) {
     auto fn = mdsx::batch::encode_tiled();
     if (!fn) return bfail(b, MDSX_ECUDA, "cuTensorMapEncodeTiled unavailable from the driver");
     cuuint64_t gdim[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
@@ -282,7 +304,7 @@ int make_tmap(mdsx_batch* b, CUtensorMap* map, void* base, long long cols, long 
     cuuint32_t box[2] = {box_cols, box_rows};
     cuuint32_t estride[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, gdim, gstride, box, estride,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return bfail(b, MDSX_ECUDA, "cuTensorMapEncodeTiled failed");
     return MDSX_OK;
@@ -303,18 +325,129 @@ void set_precision_constants(D& d, double tau) {
     d.ts2 = (float)(mdsx::kTailS2 / s);
 }
 
-// Missing-row flags into row P of the SoA location array (read by the queue
-// schedule with the row block's locations): 1 for rows whose delta row has a NaN.
-__global__ void flag_rows_kernel(const int* __restrict__ row_nan, int n, float* __restrict__ flags) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) flags[i] = row_nan[i] ? 1.0f : 0.0f;
+// Unordered-pair schedule of one group: the members' unit lists (pair_kernel.cuh)
+// concatenated in member order and split over the group's CTAs (all SMs at the
+// group's occupancy) by modelled cost (pair_unit_cost); per member the slot
+// tables of its column blocks, its partial buffers, tensor maps and a PairArgs
+// descriptor.
+int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
+    using mdsx::pair_unit_cost;
+    using mdsx::pair_units_before;
+    struct Geo {
+        int nb, nc;
+        long long units, begin;
+    };
+    std::vector<Geo> geo;
+    long long U = 0;
+    double total = 0.0;
+    for (int k : g.members) {
+        const BatchInst& in = b->inst[k];
+        Geo q;
+        q.nb = (in.n + mdsx::kPairCols - 1) / mdsx::kPairCols;
+        q.nc = (in.n + mdsx::kPairRows - 1) / mdsx::kPairRows;
+        q.units = pair_units_before(q.nb, q.nc);
+        q.begin = U;
+        U += q.units;
+        for (int J = 0; J < q.nb; ++J)
+            for (int I = 4 * J; I < q.nc; ++I) total += pair_unit_cost(I, J);
+        geo.push_back(q);
+    }
+    g.n_units = U;
+    const int G = (int)std::min<long long>(U, (long long)b->sm_count * g.ctas_per_sm);
+    g.grid = G;
+    // cost-balanced CTA ranges, strictly increasing with room for the ranges after each
+    std::vector<long long> begin(G + 1);
+    {
+        int c = 1;
+        double cum = 0.0;
+        long long u = 0;
+        begin[0] = 0;
+        for (size_t m = 0; m < geo.size() && c < G; ++m)
+            for (int J = 0; J < geo[m].nb && c < G; ++J)
+                for (int I = 4 * J; I < geo[m].nc && c < G; ++I, ++u) {
+                    while (c < G && cum >= total * c / G) begin[c++] = u;
+                    cum += pair_unit_cost(I, J);
+                }
+        while (c < G) begin[c++] = U;
+        begin[G] = U;
+        for (int k = 1; k < G; ++k) begin[k] = std::min(std::max(begin[k], begin[k - 1] + 1), U - (G - k));
+    }
+    auto cta_of = [&](long long u) {  // CTA whose range holds global unit u
+        return (int)(std::upper_bound(begin.begin(), begin.end(), u) - begin.begin()) - 1;
+    };
+    cudaStream_t st = b->stream;
+    int finish = 0;
+    for (size_t m = 0; m < g.members.size(); ++m) {
+        BatchInst& in = b->inst[g.members[m]];
+        const Geo& q = geo[m];
+        std::vector<int> jfirst(q.nb), jslots(q.nb);
+        int max_slots = 1;
+        for (int J = 0; J < q.nb; ++J) {
+            const long long u0 = q.begin + pair_units_before(J, q.nc);
+            const long long u1 = u0 + (q.nc - 4 * J) - 1;
+            jfirst[J] = cta_of(u0);
+            jslots[J] = cta_of(u1) - jfirst[J] + 1;
+            max_slots = std::max(max_slots, jslots[J]);
+        }
+        const int first_cta = cta_of(q.begin);
+        const int islots = cta_of(q.begin + q.units - 1) - first_cta + 1;
+        BCUDA(b, cudaMalloc(&in.d_prow, (size_t)q.units * mdsx::kPairRows * g.p * sizeof(float)));
+        BCUDA(b, cudaMalloc(&in.d_pcol,
+                            (size_t)q.nb * max_slots * mdsx::kPairWarps * g.p * mdsx::kPairCols * sizeof(float)));
+        BCUDA(b, cudaMalloc(&in.d_plp, (size_t)islots * mdsx::kPairWarps * 2 * sizeof(double)));
+        BCUDA(b, cudaMalloc(&in.d_pjfirst, (size_t)q.nb * sizeof(int)));
+        BCUDA(b, cudaMalloc(&in.d_pjslots, (size_t)q.nb * sizeof(int)));
+        BCUDA(b, cudaMemcpyAsync(in.d_pjfirst, jfirst.data(), (size_t)q.nb * sizeof(int), cudaMemcpyHostToDevice, st));
+        BCUDA(b, cudaMemcpyAsync(in.d_pjslots, jslots.data(), (size_t)q.nb * sizeof(int), cudaMemcpyHostToDevice, st));
+        BCUDA(b, cudaStreamSynchronize(st));  // the host tables go out of scope
+        mdsx::batch::PairInstance d{};
+        int rc = make_tmap(b, &d.tmap_a, in.d_delta, in.n, in.n, in.ld, mdsx::kPairCols, mdsx::kPairRows);
+        if (!rc)
+            rc = make_tmap(b, &d.tmap_b, in.d_delta, in.n, in.n, in.ld, mdsx::kPairRows, mdsx::kPairCols,
+                           CU_TENSOR_MAP_SWIZZLE_128B);
+        // the location maps span x_ld columns, so the flags past N are read from memory (1), not filled
+        if (!rc) rc = make_tmap(b, &d.tmap_xi, in.d_x, in.x_ld, g.p + 1, in.x_ld, mdsx::kPairRows, g.p + 1);
+        if (!rc) rc = make_tmap(b, &d.tmap_xj, in.d_x, in.x_ld, g.p + 1, in.x_ld, mdsx::kPairCols, g.p + 1);
+        if (rc) return rc;
+        mdsx::PairArgs& a = d.args;
+        a.n = in.n;
+        a.nb = q.nb;
+        a.nc = q.nc;
+        a.grid = islots;
+        a.max_slots = max_slots;
+        a.truncation = g.trunc ? 1 : 0;
+        a.n_units = q.units;
+        set_precision_constants(a, in.tau);
+        a.sqrt_tau = std::sqrt(in.tau);
+        a.rowpart = in.d_prow;
+        a.colpart = in.d_pcol;
+        a.lpart = in.d_plp;
+        a.j_first_cta = in.d_pjfirst;
+        a.j_slots = in.d_pjslots;
+        d.unit_begin = q.begin;
+        d.first_cta = first_cta;
+        d.finish_begin = finish;
+        finish += q.nc + 1;
+        g.h_pdesc.push_back(d);
+    }
+    g.finish_blocks = finish;
+    BCUDA(b, cudaMalloc(&g.d_pdesc, g.h_pdesc.size() * sizeof(mdsx::batch::PairInstance)));
+    BCUDA(b, cudaMalloc(&g.d_pbegin, (size_t)(G + 1) * sizeof(long long)));
+    BCUDA(b, cudaMemcpy(g.d_pbegin, begin.data(), (size_t)(G + 1) * sizeof(long long), cudaMemcpyHostToDevice));
+    return MDSX_OK;
 }
 
-// Shape of a group: the override, else the tuning cache, else the default
-// (row-block queue, the single-instance rows per warp, full occupancy).
+// Shape of a group: the override, else the tuning cache, else the default: with
+// truncation and P <= 4 the unordered-pair schedule (the single-instance
+// engine's choice), otherwise the row-block queue with the single-instance rows
+// per warp; full occupancy.
 Shape group_shape(const mdsx_batch* b, int p, double mean_n, const std::map<std::pair<int, int>, Shape>* force) {
     Shape sh;
     sh.rw = mdsx::batch::default_rw(p);
+    if (b->trunc && p <= mdsx::kPairMaxP) {
+        sh.schedule = 2;
+        sh.rw = 4;
+    }
     {
         std::lock_guard<std::mutex> lock(mdsx::batch::g_tune_mu);
         mdsx::batch::load_cache_locked();
@@ -363,8 +496,10 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
         size_t local = 0;
         if (sh.schedule == 0)
             BCUDA(b, mdsx::batch::occupancy(g.p, g.trunc, sh.rw, &occ, &local));
-        else
+        else if (sh.schedule == 1)
             BCUDA(b, mdsx::batch::occupancy_queue(g.p, g.trunc, sh.rw, &occ));
+        else
+            BCUDA(b, mdsx::batch::occupancy_pairs(g.p, g.trunc, &occ));
         if (occ < 1) return bfail(b, MDSX_ECUDA, "batched sweep kernel cannot be resident");
         g.schedule = sh.schedule;
         g.rw = sh.rw;
@@ -379,8 +514,9 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
             in.rows_padded = in.n_row_blocks * rb;
             BCUDA(b, cudaMalloc(&in.d_row_nan, (size_t)in.rows_padded * sizeof(int)));
             BCUDA(b, mdsx::mark_nan_rows(in.d_delta, true, in.n, in.ld, in.d_row_nan, in.rows_padded, st));
-            flag_rows_kernel<<<(in.n + 255) / 256, 256, 0, st>>>(in.d_row_nan, in.n, in.d_x + (size_t)g.p * in.x_ld);
-            BCUDA(b, cudaGetLastError());
+            // flag row: 1 for rows with a NaN and for columns n .. x_ld (read by the pair schedule)
+            BCUDA(b, mdsx::write_flag_row(in.d_row_nan, in.n, in.rows_padded, in.d_x + (size_t)g.p * in.x_ld, true,
+                                          in.x_ld, st));
         }
         if (g.schedule == 0) {
             // stream-K: global units, slots, scratch
@@ -428,6 +564,11 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
                 d.done_count = in.d_counts + d.n_row_blocks;
             }
             BCUDA(b, cudaMalloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
+        } else if (g.schedule == 2) {
+            // full residency, as the queue: the CTAs never wait on one another, so
+            // concurrent groups simply share the SMs
+            int rc = plan_pairs_group(b, g);
+            if (rc) return rc;
         } else {
             // row-block queue: items ordered largest instance first
             g.order = g.members;
@@ -477,6 +618,12 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
             g.h_qdesc[m].grad_out = b->d_grad_all + b->inst[k].grad_off;
             g.h_qdesc[m].sums_out = b->d_sums_all + 4 * (size_t)k;
         }
+        for (size_t m = 0; m < g.h_pdesc.size(); ++m) {
+            const int k = g.members[m];
+            g.h_pdesc[m].args.grad_out = b->d_grad_all + b->inst[k].grad_off;
+            g.h_pdesc[m].args.sums_out = b->d_sums_all + 4 * (size_t)k;
+            g.h_pdesc[m].args.err = b->d_err;
+        }
     }
     while (b->aux.size() < b->groups.size()) {  // branch streams for concurrent groups (created outside capture)
         cudaStream_t bs = nullptr;
@@ -503,6 +650,9 @@ int upload_descriptors(mdsx_batch* b) {
         if (!g.h_qdesc.empty())
             BCUDA(b, cudaMemcpyAsync(g.d_qdesc, g.h_qdesc.data(), g.h_qdesc.size() * sizeof(mdsx::batch::QueueInstance),
                                      cudaMemcpyHostToDevice, b->stream));
+        if (!g.h_pdesc.empty())
+            BCUDA(b, cudaMemcpyAsync(g.d_pdesc, g.h_pdesc.data(), g.h_pdesc.size() * sizeof(mdsx::batch::PairInstance),
+                                     cudaMemcpyHostToDevice, b->stream));
     }
     BCUDA(b, cudaStreamSynchronize(b->stream));  // the host descriptors may change after return
     b->desc_dirty = false;
@@ -523,6 +673,15 @@ BatchArgs group_args(const mdsx_batch* b, const BatchGroup& g) {
 int launch_group(mdsx_batch* b, const BatchGroup& g, cudaStream_t st) {
     if (g.schedule == 0) {
         BCUDA(b, mdsx::batch::launch(g.p, g.trunc, g.rw, group_args(b, g), st));
+        return MDSX_OK;
+    }
+    if (g.schedule == 2) {
+        mdsx::batch::BatchPairArgs a{};
+        a.inst = g.d_pdesc;
+        a.count = (int)g.h_pdesc.size();
+        a.cta_begin = g.d_pbegin;
+        a.err = b->d_err;
+        BCUDA(b, mdsx::batch::launch_pairs(g.p, g.trunc, a, g.grid, g.finish_blocks, st));
         return MDSX_OK;
     }
     mdsx::batch::QueueArgs a{};
@@ -743,6 +902,11 @@ int mdsx_batch_set_parameters(mdsx_batch* b, int k, const double* parameters, si
             if (g.members[m] == k) set_precision_constants(g.h_desc[m], parameters[0]);
         for (size_t m = 0; m < g.h_qdesc.size(); ++m)
             if (g.order[m] == k) set_precision_constants(g.h_qdesc[m], parameters[0]);
+        for (size_t m = 0; m < g.h_pdesc.size(); ++m)
+            if (g.members[m] == k) {
+                set_precision_constants(g.h_pdesc[m].args, parameters[0]);
+                g.h_pdesc[m].args.sqrt_tau = std::sqrt(parameters[0]);
+            }
     }
     b->desc_dirty = true;
     b->results_known = false;
@@ -891,8 +1055,8 @@ int time_group(mdsx_batch* b, const BatchGroup& g, int reps, double* us) {
 extern "C" {
 
 // Test and tuning hook: fixes the shape of the group of embedding dimension p:
-// schedule (0 stream-K, 1 row-block queue), rows per warp, CTAs per SM;
-// rows_per_warp 0 removes the override.
+// schedule (0 stream-K, 1 row-block queue, 2 unordered pairs with rows per warp 4,
+// P <= 4), rows per warp, CTAs per SM; rows_per_warp 0 removes the override.
 int mdsx_batch_force_shape(mdsx_batch* b, int p, int schedule, int rows_per_warp, int ctas_per_sm) {
     if (!b) return MDSX_EINVAL;
     const std::pair<int, int> key{p, b->trunc ? 1 : 0};
@@ -900,9 +1064,11 @@ int mdsx_batch_force_shape(mdsx_batch* b, int p, int schedule, int rows_per_warp
         b->forced.erase(key);
     } else {
         if (!mdsx::batch::rw_built(p, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4 ||
-            (schedule != 0 && schedule != 1))
+            (schedule != 0 && schedule != 1 && schedule != 2) ||
+            (schedule == 2 && (p > mdsx::kPairMaxP || rows_per_warp != 4)))
             return bfail(b, MDSX_EINVAL,
-                         "schedule not 0 or 1, rows per warp not built for this dimension, or CTAs per SM outside 1..4");
+                         "schedule not 0, 1 or 2, rows per warp not built for this dimension and schedule, or CTAs per "
+                         "SM outside 1..4");
         b->forced[key] = Shape{schedule, rows_per_warp, ctas_per_sm};
     }
     free_plan(b);
@@ -933,17 +1099,18 @@ int mdsx_batch_tune(mdsx_batch* b, int repetitions, int* candidates) {
     int timed = 0;
     std::map<std::pair<int, int>, Shape> best_shape;
     std::map<std::pair<int, int>, double> best_us;
-    for (int sched : {0, 1})
+    for (int sched : {0, 1, 2})
         for (int rw : {1, 2, 4})
             for (int ctas : {1, 2}) {
                 std::map<std::pair<int, int>, Shape> force;
                 bool any = false;
                 for (const auto& k : keys)
-                    if (mdsx::batch::rw_built(k.p, rw)) {
+                    if (mdsx::batch::rw_built(k.p, rw) && (sched != 2 || (rw == 4 && k.p <= mdsx::kPairMaxP))) {
                         int occ = 0;
                         size_t local = 0;
-                        const cudaError_t ce = sched == 0 ? mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local)
-                                                          : mdsx::batch::occupancy_queue(k.p, k.trunc != 0, rw, &occ);
+                        const cudaError_t ce = sched == 0   ? mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local)
+                                               : sched == 1 ? mdsx::batch::occupancy_queue(k.p, k.trunc != 0, rw, &occ)
+                                                            : mdsx::batch::occupancy_pairs(k.p, k.trunc != 0, &occ);
                         if (ce != cudaSuccess || occ < ctas) continue;
                         force[{k.p, k.trunc}] = Shape{sched, rw, ctas};
                         any = true;

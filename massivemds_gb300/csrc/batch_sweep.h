@@ -7,6 +7,7 @@
 #include <cstddef>
 
 #include "batch_kernel.cuh"
+#include "batch_pairs.cuh"
 #include "batch_queue.cuh"
 
 namespace mdsx {
@@ -23,6 +24,11 @@ cudaError_t launch(int p, bool trunc, int rw, const BatchArgs& a, cudaStream_t s
 // Row-block queue schedule (batch_queue.cuh).
 cudaError_t occupancy_queue(int p, bool trunc, int rw, int* ctas_per_sm);
 cudaError_t launch_queue(int p, bool trunc, int rw, const QueueArgs& a, int grid, cudaStream_t st);
+
+// Unordered-pair schedule (batch_pairs.cuh, batch_sweep_pairs.cu): P <= kPairMaxP.
+cudaError_t occupancy_pairs(int p, bool trunc, int* ctas_per_sm);
+// The sweep (grid CTAs) and its finish kernel (finish_blocks blocks) as a programmatic dependent.
+cudaError_t launch_pairs(int p, bool trunc, const BatchPairArgs& a, int grid, int finish_blocks, cudaStream_t st);
 
 #define MDSX_BATCH_DECLARE(R)                                                                  \
     cudaError_t occupancy_##R(int p, bool trunc, int rw, int* ctas_per_sm, size_t* local_bytes); \

@@ -689,15 +689,15 @@ struct FinishShape {
     static constexpr int kChunk = 8;                 // loads in flight per thread
 };
 
+// Block `blk` of the finish of one sweep (block 0: likelihood; block nc - I: row chunk I).
 template <int P, typename Part>
-__global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
+__device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
     using FS = FinishShape<P>;
     const Part* rowpart = static_cast<const Part*>(a.rowpart);
     const Part* colpart = static_cast<const Part*>(a.colpart);
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     __shared__ double part[2][FS::kThreads];
     const int t = threadIdx.x;
-    if (blockIdx.x == 0) {
+    if (blk == 0) {
         const int total = a.grid * kPairWarps;
         double s0 = 0.0, s1 = 0.0;
         for (int e0 = t; e0 < total; e0 += FS::kThreads * 8) {
@@ -734,7 +734,7 @@ __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
         }
         return;
     }
-    const int I = a.nc - (int)blockIdx.x;  // the chunks with the most partials are scheduled first
+    const int I = a.nc - blk;  // the chunks with the most partials are scheduled first
     const int g = t / FS::kOut, o = t - g * FS::kOut;  // o = r * P + q
     double acc = 0.0;
     if (g < FS::kGroups) {
@@ -775,6 +775,12 @@ __global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
         const int row = I * kPairRows + t / P;
         if (row < a.n) a.grad_out[(size_t)I * FS::kOut + t] = a.tau * s;
     }
+}
+
+template <int P, typename Part>
+__global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    pair_finish_block<P, Part>(a, (int)blockIdx.x);
 }
 
 }  // namespace mdsx

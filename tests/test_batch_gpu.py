@@ -1,9 +1,10 @@
 """GPU parity tests of the batched multi-instance engine (batch.cu,
-batch_kernel.cuh) against the oracle, instance by instance: every instance's
-sum of increments and gradient within 1e-5 relative of the FP64 oracle on its
-FP32-rounded delta (the FP32 bar of the single-instance engine), for uneven N,
-mixed P, both schedules and every built tile shape, missing pairs, single-location updates and
-precision changes; plus determinism and the autotuner."""
+batch_kernel.cuh, batch_queue.cuh, batch_pairs.cuh) against the oracle,
+instance by instance: every instance's sum of increments and gradient within
+1e-5 relative of the FP64 oracle on its FP32-rounded delta (the FP32 bar of the
+single-instance engine), for uneven N, mixed P, the three schedules and every
+built tile shape, missing pairs, single-location updates and precision
+changes; plus determinism and the autotuner."""
 import numpy as np
 import pytest
 
@@ -79,15 +80,64 @@ def test_every_shape_matches_oracle(schedule, p, rw, ctas):
         _check(b, problems)
 
 
+@pytest.mark.parametrize("ctas", [1, 2])
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_pair_schedule_matches_oracle(p, ctas):
+    problems = _problems([(257, p), (640, p), (129, p), (1000, p), (33, p), (2, p)], 20 + p)
+    with Batch() as b:
+        _fill(b, problems)
+        b.force_shape(p, 4, ctas, 2)
+        assert b.group_shape(p)[:3] == (2, 4, ctas)
+        _check(b, problems)
+
+
+def test_pair_schedule_mixed_groups_missing_pairs_and_updates():
+    """Pair-schedule groups (P = 2, 3) beside a row-schedule group (P = 6) in one
+    graph; asymmetric NaN pairs; precision and location updates."""
+    problems = _problems([(300, 2), (700, 3), (260, 6), (1100, 2), (450, 3)], 21)
+    d = problems[0][0].copy()
+    rng = np.random.default_rng(3)
+    for _ in range(30):
+        i, j = rng.integers(0, 300, 2)
+        d[i, j] = np.nan  # (j, i) stays observed
+    d[17, :] = np.nan
+    problems[0] = (d, problems[0][1], problems[0][2])
+    with Batch() as b:
+        _fill(b, problems)
+        b.force_shape(2, 4, 2, 2)
+        b.force_shape(3, 4, 2, 2)
+        _check(b, problems)
+        delta, x, tau = problems[3]
+        x = x.copy()
+        x[5] += 0.5
+        b.updateLocations(3, 5, x[5])
+        b.setParameters(4, [0.37])
+        problems[3] = (delta, x, tau)
+        problems[4] = (problems[4][0], problems[4][1], 0.37)
+        _check(b, problems)
+        b.makeDirty()
+        b.evaluate()
+        s1 = [b.getSumOfIncrements(k) for k in range(len(problems))]
+        g1 = [b.getLogLikelihoodGradient(k).copy() for k in range(len(problems))]
+        b.makeDirty()
+        b.evaluate()
+        assert [b.getSumOfIncrements(k) for k in range(len(problems))] == s1
+        for k in range(len(problems)):
+            assert np.array_equal(b.getLogLikelihoodGradient(k), g1[k])
+
+
 def test_schedules_agree_and_gradients_concatenate_in_instance_order():
     torch = pytest.importorskip("torch")
     problems = _problems([(300, 6), (700, 2), (451, 3), (1200, 2)], 12)
     grads = {}
-    for schedule in (0, 1):
+    for schedule in (0, 1, 2):
         with Batch() as b:
             _fill(b, problems)
             for p in (2, 3, 6):
-                b.force_shape(p, 1, 2, schedule)
+                if schedule == 2:
+                    b.force_shape(p, 4, 2, 2) if p <= 4 else b.force_shape(p, 1, 2, 0)
+                else:
+                    b.force_shape(p, 1, 2, schedule)
             total = sum(x.size for _, x, _ in problems)
             d_sums = torch.zeros(4 * len(problems), dtype=torch.float64, device="cuda")
             d_grads = torch.zeros(total, dtype=torch.float64, device="cuda")
@@ -99,8 +149,9 @@ def test_schedules_agree_and_gradients_concatenate_in_instance_order():
                 assert np.array_equal(g[off:off + x.size], b.getLogLikelihoodGradient(k))
                 off += x.size
             grads[schedule] = g
-    # same tile shape, two schedules: the row partials are summed in different orders
-    assert np.abs(grads[0] - grads[1]).max() <= 1e-5 * np.abs(grads[1]).max()
+    # the schedules sum the partials in different orders
+    for schedule in (1, 2):
+        assert np.abs(grads[0] - grads[schedule]).max() <= 1e-5 * np.abs(grads[0]).max()
 
 
 def test_without_truncation():
@@ -170,5 +221,6 @@ def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
         assert b.tune(repetitions=3) >= 3
         for p in (2, 3, 6):
             sc, rw, ctas, grid = b.group_shape(p)
-            assert sc in (0, 1) and rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
+            assert sc in (0, 1, 2) and rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
+            assert sc != 2 or (p <= 4 and rw == 4)
         _check(b, problems)
