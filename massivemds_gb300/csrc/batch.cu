@@ -46,6 +46,13 @@ bool rw_built(int p, int rw) {
     return rw == 1 || (rw == 2 && p <= 8) || (rw == 4 && p <= 4);
 }
 
+// Shapes the kernels are built for: schedules 0 and 1 with rw_built rows per
+// warp; schedule 2 (unordered pairs) with 4 rows per warp and P <= kPairMaxP.
+bool shape_built(int p, int schedule, int rw) {
+    if (schedule == 2) return rw == 4 && p >= 1 && p <= kPairMaxP;
+    return (schedule == 0 || schedule == 1) && rw_built(p, rw);
+}
+
 int smem_bytes(int p, int rw) {
     const int rb = 8 * rw;
     return kStages * (rb * kStepCols * 4 + p * kStepCols * 4) + 2 * kStages * 8 + 128;
@@ -97,7 +104,7 @@ void load_cache_locked() {
     int p, b, t, sc, rw, c;
     double us;
     while (std::fscanf(f, "%d %d %d %d %d %d %lf", &p, &b, &t, &sc, &rw, &c, &us) == 7)
-        if (rw_built(p, rw) && c >= 1 && c <= 4 && (sc == 0 || sc == 1)) g_tune[{p, b, t}] = {sc, rw, c, us};
+        if (shape_built(p, sc, rw) && c >= 1 && c <= 4) g_tune[{p, b, t}] = {sc, rw, c, us};
     std::fclose(f);
 }
 
@@ -1063,9 +1070,7 @@ int mdsx_batch_force_shape(mdsx_batch* b, int p, int schedule, int rows_per_warp
     if (rows_per_warp == 0) {
         b->forced.erase(key);
     } else {
-        if (!mdsx::batch::rw_built(p, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4 ||
-            (schedule != 0 && schedule != 1 && schedule != 2) ||
-            (schedule == 2 && (p > mdsx::kPairMaxP || rows_per_warp != 4)))
+        if (!mdsx::batch::shape_built(p, schedule, rows_per_warp) || ctas_per_sm < 1 || ctas_per_sm > 4)
             return bfail(b, MDSX_EINVAL,
                          "schedule not 0, 1 or 2, rows per warp not built for this dimension and schedule, or CTAs per "
                          "SM outside 1..4");
@@ -1105,7 +1110,7 @@ int mdsx_batch_tune(mdsx_batch* b, int repetitions, int* candidates) {
                 std::map<std::pair<int, int>, Shape> force;
                 bool any = false;
                 for (const auto& k : keys)
-                    if (mdsx::batch::rw_built(k.p, rw) && (sched != 2 || (rw == 4 && k.p <= mdsx::kPairMaxP))) {
+                    if (mdsx::batch::shape_built(k.p, sched, rw)) {
                         int occ = 0;
                         size_t local = 0;
                         const cudaError_t ce = sched == 0   ? mdsx::batch::occupancy(k.p, k.trunc != 0, rw, &occ, &local)

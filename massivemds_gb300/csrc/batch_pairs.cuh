@@ -54,7 +54,7 @@ __device__ __forceinline__ int pair_find_instance(const PairInstance* inst, int 
 
 template <int P, bool TRUNC>
 __global__ void __launch_bounds__(kPairThreads, 2) batch_pair_kernel(const BatchPairArgs ba) {
-    using M = PairMathF32<P, TRUNC>;
+    using M = PairMathF32For<P, TRUNC>;
     using Shape = PairShape<P, 4, 4>;
     constexpr int S = Shape::kStages;
     extern __shared__ unsigned char smem_raw[];

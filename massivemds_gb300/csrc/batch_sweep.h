@@ -15,6 +15,8 @@ namespace batch {
 
 // Rows per warp built for P: {1, 2, 4} for P <= 4, {1, 2} for P <= 8, {1} above.
 bool rw_built(int p, int rw);
+// (schedule, rows per warp) built for P: rw_built for schedules 0 and 1; schedule 2 with 4 and P <= kPairMaxP.
+bool shape_built(int p, int schedule, int rw);
 // Dynamic shared memory of one CTA.
 int smem_bytes(int p, int rw);
 // Resident CTAs per SM and local (spill) bytes per thread of the kernel.

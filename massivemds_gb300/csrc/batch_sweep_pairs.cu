@@ -66,6 +66,8 @@ cudaError_t occupancy_pairs(int p, bool trunc, int* ctas_per_sm) {
         case 2: return occupancy_p<2>(trunc, ctas_per_sm);
         case 3: return occupancy_p<3>(trunc, ctas_per_sm);
         case 4: return occupancy_p<4>(trunc, ctas_per_sm);
+        case 5: return occupancy_p<5>(trunc, ctas_per_sm);
+        case 6: return occupancy_p<6>(trunc, ctas_per_sm);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -76,6 +78,8 @@ cudaError_t launch_pairs(int p, bool trunc, const BatchPairArgs& a, int grid, in
         case 2: return launch_p<2>(trunc, a, grid, finish_blocks, st);
         case 3: return launch_p<3>(trunc, a, grid, finish_blocks, st);
         case 4: return launch_p<4>(trunc, a, grid, finish_blocks, st);
+        case 5: return launch_p<5>(trunc, a, grid, finish_blocks, st);
+        case 6: return launch_p<6>(trunc, a, grid, finish_blocks, st);
         default: return cudaErrorInvalidValue;
     }
 }

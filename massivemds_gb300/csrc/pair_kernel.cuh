@@ -45,6 +45,8 @@
 #include <cstdint>
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "ptx.cuh"
 #include "sweep_kernel.cuh"
 
@@ -54,7 +56,8 @@ constexpr int kPairCols = 128;  // columns per block J: 32 lanes x 4
 constexpr int kPairRows = 32;   // rows per chunk I: 8 warps x 4
 constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
-constexpr int kPairMaxP = 4;
+constexpr int kPairMaxP = 6;     // FP32 pair math: P <= 4 row packs (PairMathF32), 5..6 column packs
+constexpr int kPairMaxP64 = 4;   // FP64 pair math
 
 // XB: bytes per location element (4: FP32 math, 8: FP64 math); SB: bytes per
 // delta element. FP64 math is bound by the FP64 pipe, so two stages hide the
@@ -329,6 +332,101 @@ struct PairMathF32 {
         lsum = TRUNC ? -0.69314718055994530942 * (2.0 * ((double)s.l2_hi + (double)s.l2_lo) + (double)s.l1) : 0.0;
     }
 };
+
+// FP32 policy for larger P (5, 6): a pack is two columns of one row, so a lane
+// keeps only its column sums and x_j (two column-pair packs x P) for the block
+// and one row's x_i and row sums at a time. Columns (l, l+32) and (l+64, l+96)
+// form the two column pairs; B rows come as 128-bit loads of four rows each,
+// and a pack takes the same row from two of them.
+template <int P, bool TRUNC>
+struct PairMathF32Cols {
+    using X = float;
+    using S = float;
+    using Part = float;
+    static constexpr int kFoldUnits = 4;  // per half: 16 r^2 terms and 8 factors of 1/Phi per unit
+    struct Cols {
+        f2 nxj[2][P];  // (-x_j, -x_j') of columns (l + 64 cp, l + 64 cp + 32)
+        f2 acc[2][P];
+    };
+    using Sums = typename PairMathF32<P, TRUNC>::Sums;
+    PairConstsF32 k;
+
+    __device__ explicit PairMathF32Cols(const PairArgs& a)
+        : k{pk(-1.f, -1.f),     pk(a.k_e, a.k_e),   pk(a.log2_k2, a.log2_k2), pk(-a.tp0, -a.tp0), pk(-a.tp1, -a.tp1),
+            pk(-a.tp2, -a.tp2), pk(a.ts0, a.ts0), pk(a.ts1, a.ts1),         pk(a.ts2, a.ts2)} {}
+
+    __device__ static void init(Sums& s) { PairMathF32<P, TRUNC>::init(s); }
+    __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
+#pragma unroll
+        for (int cp = 0; cp < 2; ++cp)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                cols.nxj[cp][q] = pk(-sXJ[q * kPairCols + lane + 64 * cp], -sXJ[q * kPairCols + lane + 64 * cp + 32]);
+                cols.acc[cp][q] = pk(0.f, 0.f);
+            }
+    }
+    template <bool MASKED>
+    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
+                         int lane, int warp, Part (&v)[4 * P]) const {
+        // B rows l + 32 c, chunk w (rows 4w .. 4w+3 of the chunk), 128-byte swizzle
+        const float* sBl = sB + lane * kPairRows + ((warp ^ (lane & 7)) << 2);
+        float4 b[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+        f2 prodm = pk(1.f, 1.f);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            f2 xi[P], racc[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const float x = sXI[q * kPairRows + 4 * warp + r];
+                xi[q] = pk(x, x);
+                racc[q] = pk(0.f, 0.f);
+            }
+            const int i = i0 + r;
+#pragma unroll
+            for (int cp = 0; cp < 2; ++cp) {
+                const float a0 = sA[(4 * warp + r) * kPairCols + lane + 64 * cp];
+                const float a1 = sA[(4 * warp + r) * kPairCols + lane + 64 * cp + 32];
+                const float4& b0 = b[2 * cp];
+                const float4& b1 = b[2 * cp + 1];
+                const float d0 = r == 0 ? b0.x : r == 1 ? b0.y : r == 2 ? b0.z : b0.w;
+                const float d1 = r == 0 ? b1.x : r == 1 ? b1.y : r == 2 ? b1.z : b1.w;
+                bool vA0 = true, vA1 = true, vB0 = true, vB1 = true;
+                if (MASKED) {
+                    const int j = j0 + lane + 64 * cp;
+                    const bool ok0 = (i < n) && (j < n) && (i > j);
+                    const bool ok1 = (i < n) && (j + 32 < n) && (i > j + 32);
+                    vA0 = ok0 && (a0 == a0);
+                    vA1 = ok1 && (a1 == a1);
+                    vB0 = ok0 && (d0 == d0);
+                    vB1 = ok1 && (d1 == d1);
+                }
+                pair_pack<P, TRUNC, MASKED>(xi, cols.nxj[cp], pk(a0, a1), pk(d0, d1), vA0, vA1, vB0, vB1, k, racc,
+                                            cols.acc[cp], s.r2, s.prod, prodm);
+            }
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[r * P + q] = sum2(racc[q]);
+        }
+        if (MASKED && TRUNC) {
+            float m0, m1;
+            upk(prodm, m0, m1);
+            s.l1 += lg2_approx(m0) + lg2_approx(m1);  // <= 16 factors in [1, 2] per half
+        }
+    }
+    __device__ static void after_unit(Sums& s) { PairMathF32<P, TRUNC>::after_unit(s); }
+    __device__ static Part col_value(const Cols& cols, int c, int q) {
+        float lo, hi;
+        upk(cols.acc[c >> 1][q], lo, hi);
+        return (c & 1) ? hi : lo;
+    }
+    __device__ static void result(Sums& s, double& r2, double& lsum) { PairMathF32<P, TRUNC>::result(s, r2, lsum); }
+};
+
+// The FP32 policy for P.
+template <int P, bool TRUNC>
+using PairMathF32For =
+    typename std::conditional<(P <= 4), PairMathF32<P, TRUNC>, PairMathF32Cols<P, TRUNC>>::type;
 
 // ------------------------------------------------------------ FP64 pair math
 

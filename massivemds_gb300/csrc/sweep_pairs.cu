@@ -1,6 +1,6 @@
 // Instances of the unordered-pair sweep (pair_kernel.cuh) -- FP32 pair math
 // (FP32 mode), FP64 pair math over FP32-stored delta (DELTA_F32 mode) and over
-// FP64-stored delta (default mode), P = 1..kPairMaxP, truncation on/off -- and
+// FP64-stored delta (default mode), P = 1..kPairMaxP (FP32) / kPairMaxP64 (FP64), truncation on/off -- and
 // the host-side launch of the sweep and its finish kernel.
 #include <type_traits>
 
@@ -13,7 +13,7 @@ namespace {
 // MODE: 0 FP32 math, 1 FP64 math over FP32 delta, 2 FP64 math over FP64 delta.
 template <int P, bool TRUNC, int MODE>
 using MathOf = typename std::conditional<
-    MODE == 0, PairMathF32<P, TRUNC>,
+    MODE == 0, PairMathF32For<P, TRUNC>,
     typename std::conditional<MODE == 1, PairMathF64<P, TRUNC, float>, PairMathF64<P, TRUNC, double>>::type>::type;
 
 template <int P, bool TRUNC, int MODE>
@@ -74,10 +74,15 @@ cudaError_t pair_launch_pm(bool trunc, const PairMaps& maps, const PairArgs& arg
 
 template <int P>
 cudaError_t pair_launch_p(bool trunc, int mode, const PairMaps& maps, const PairArgs& args, cudaStream_t stream) {
-    switch (mode) {
-        case 0: return pair_launch_pm<P, 0>(trunc, maps, args, stream);
-        case 1: return pair_launch_pm<P, 1>(trunc, maps, args, stream);
-        default: return pair_launch_pm<P, 2>(trunc, maps, args, stream);
+    if constexpr (P > kPairMaxP64) {
+        if (mode != 0) return cudaErrorInvalidValue;
+        return pair_launch_pm<P, 0>(trunc, maps, args, stream);
+    } else {
+        switch (mode) {
+            case 0: return pair_launch_pm<P, 0>(trunc, maps, args, stream);
+            case 1: return pair_launch_pm<P, 1>(trunc, maps, args, stream);
+            default: return pair_launch_pm<P, 2>(trunc, maps, args, stream);
+        }
     }
 }
 
@@ -88,16 +93,21 @@ cudaError_t pair_occupancy_pm(bool trunc, int* ctas) {
 
 template <int P>
 cudaError_t pair_occupancy_p(bool trunc, int mode, int* ctas) {
-    switch (mode) {
-        case 0: return pair_occupancy_pm<P, 0>(trunc, ctas);
-        case 1: return pair_occupancy_pm<P, 1>(trunc, ctas);
-        default: return pair_occupancy_pm<P, 2>(trunc, ctas);
+    if constexpr (P > kPairMaxP64) {
+        if (mode != 0) return cudaErrorInvalidValue;
+        return pair_occupancy_pm<P, 0>(trunc, ctas);
+    } else {
+        switch (mode) {
+            case 0: return pair_occupancy_pm<P, 0>(trunc, ctas);
+            case 1: return pair_occupancy_pm<P, 1>(trunc, ctas);
+            default: return pair_occupancy_pm<P, 2>(trunc, ctas);
+        }
     }
 }
 
 }  // namespace
 
-bool pair_built(Mode, int p) { return p >= 1 && p <= kPairMaxP; }
+bool pair_built(Mode mode, int p) { return p >= 1 && p <= (mode == Mode::kF32 ? kPairMaxP : kPairMaxP64); }
 
 cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm) {
     const int m = mode_index(mode);
@@ -106,6 +116,8 @@ cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm) {
         case 2: return pair_occupancy_p<2>(trunc, m, ctas_per_sm);
         case 3: return pair_occupancy_p<3>(trunc, m, ctas_per_sm);
         case 4: return pair_occupancy_p<4>(trunc, m, ctas_per_sm);
+        case 5: return pair_occupancy_p<5>(trunc, m, ctas_per_sm);
+        case 6: return pair_occupancy_p<6>(trunc, m, ctas_per_sm);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -118,6 +130,8 @@ cudaError_t pair_launch(int p, bool trunc, Mode mode, const PairMaps& maps, cons
         case 2: return pair_launch_p<2>(trunc, m, maps, args, stream);
         case 3: return pair_launch_p<3>(trunc, m, maps, args, stream);
         case 4: return pair_launch_p<4>(trunc, m, maps, args, stream);
+        case 5: return pair_launch_p<5>(trunc, m, maps, args, stream);
+        case 6: return pair_launch_p<6>(trunc, m, maps, args, stream);
         default: return cudaErrorInvalidValue;
     }
 }

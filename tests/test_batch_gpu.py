@@ -81,7 +81,7 @@ def test_every_shape_matches_oracle(schedule, p, rw, ctas):
 
 
 @pytest.mark.parametrize("ctas", [1, 2])
-@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5, 6])
 def test_pair_schedule_matches_oracle(p, ctas):
     problems = _problems([(257, p), (640, p), (129, p), (1000, p), (33, p), (2, p)], 20 + p)
     with Batch() as b:
@@ -135,7 +135,7 @@ def test_schedules_agree_and_gradients_concatenate_in_instance_order():
             _fill(b, problems)
             for p in (2, 3, 6):
                 if schedule == 2:
-                    b.force_shape(p, 4, 2, 2) if p <= 4 else b.force_shape(p, 1, 2, 0)
+                    b.force_shape(p, 4, 2, 2)
                 else:
                     b.force_shape(p, 1, 2, schedule)
             total = sum(x.size for _, x, _ in problems)
@@ -222,5 +222,5 @@ def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
         for p in (2, 3, 6):
             sc, rw, ctas, grid = b.group_shape(p)
             assert sc in (0, 1, 2) and rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
-            assert sc != 2 or (p <= 4 and rw == 4)
+            assert sc != 2 or (p <= 6 and rw == 4)
         _check(b, problems)

@@ -152,8 +152,8 @@ def test_sizes_and_edges(mode, n):
 @pytest.mark.parametrize("mode", ["f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32pairs"])
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_dimensions(mode, p):
-    if mode.endswith("pairs") and p > 4:
-        pytest.skip("the unordered-pair schedule is built for P <= 4")
+    if mode.endswith("pairs") and p > (6 if mode == "f32pairs" else 4):
+        pytest.skip("the unordered-pair schedule is built for P <= 6 (FP32) and P <= 4 (FP64)")
     n, tau = 300, 0.8
     delta, x = _inputs(n, p, seed=100 + p, nans=2, asym=True)
     tol_s, tol_g = tolerances(mode)
@@ -298,10 +298,11 @@ def test_error_statuses():
 
 
 def test_sweep_schedules():
-    """Truncated engines with P <= 4 (every precision mode) default to the
-    unordered-pair schedule (sweep + finish kernel), untruncated ones to the
-    row-block schedule; P > 4 runs the row-block schedule and refuses the pair
-    schedule; switching invalidates the cached results."""
+    """Truncated engines default to the unordered-pair schedule (sweep + finish
+    kernel) where it is built (FP32: P <= 6; FP64: P <= 4), untruncated ones to
+    the row-block schedule; beyond that range the engine runs the row-block
+    schedule and refuses the pair schedule; switching invalidates the cached
+    results."""
     n, tau = 300, 1.3
     delta, x = _inputs(n, 2, seed=29)
     e = make_engine(n, 2, False, "f32", delta, x, tau)
@@ -309,9 +310,9 @@ def test_sweep_schedules():
     e.set_sweep_schedule(F.SWEEP_PAIRS)
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
     e.close()
-    for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (5, "f32", F.SWEEP_ROWS),
-                             (2, "f64", F.SWEEP_PAIRS), (5, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS),
-                             (5, "f64s32", F.SWEEP_ROWS)):
+    for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (6, "f32", F.SWEEP_PAIRS),
+                             (7, "f32", F.SWEEP_ROWS), (2, "f64", F.SWEEP_PAIRS), (5, "f64", F.SWEEP_ROWS),
+                             (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_ROWS)):
         delta, x = _inputs(n, p, seed=30 + p)
         e = make_engine(n, p, True, mode, delta, x, tau)
         assert e.sweep_schedule() == default, (p, mode)
