@@ -53,7 +53,7 @@ __device__ __forceinline__ int pair_find_instance(const PairInstance* inst, int 
 }
 
 template <int P, bool TRUNC>
-__global__ void __launch_bounds__(kPairThreads, 2) batch_pair_kernel(const BatchPairArgs ba) {
+__global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>()) batch_pair_kernel(const BatchPairArgs ba) {
     using M = PairMathF32For<P, TRUNC>;
     using Shape = PairShape<P, 4, 4>;
     constexpr int S = Shape::kStages;
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kPairThreads, 2) batch_pair_kernel(const Batch
             }
             const PairInstance& in = ba.inst[pk];
             unsigned char* st = smem + stage * Shape::kStageBytes;
-            const bool new_j = pJ != pJ_loaded;
+            const bool new_j = M::kXJEveryUnit || pJ != pJ_loaded;
             const uint32_t bytes =
                 Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
             mbar_arrive_expect_tx(&full[stage], bytes);
@@ -202,15 +202,8 @@ __global__ void __launch_bounds__(kPairThreads, 2) batch_pair_kernel(const Batch
                     math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&empty[stage]);
-                {
-                    constexpr int KV = 4 * P;
-                    using TS = TransposeShape<KV>;
-                    warp_transpose_reduce<KV>(v, lane);
-                    const int idx = lane >> TS::kLaneShift;
-                    const long long lu = u_begin + k - in.unit_begin;
-                    if ((lane & ((1 << TS::kLaneShift) - 1)) == 0 && idx < KV)
-                        rowpart[((size_t)lu * kPairRows + 4 * warp) * P + idx] = v[0];
-                }
+                flush_row_sums<4 * P>(v, rowpart + ((size_t)(u_begin + k - in.unit_begin) * kPairRows + 4 * warp) * P,
+                                      lane);
                 M::after_unit(sums);
             }
             if (!alive) break;

@@ -25,7 +25,8 @@
 //   x_J = the same over J's 128 columns, with the first unit of each J
 // into a ring of PairShape::kStages stages (mbarrier full/empty pairs). Lane 0
 // of warp 0 issues the copies between its own units, so all 8 warps of a CTA
-// compute and 2 CTAs of 256 threads fit an SM at 128 registers.
+// compute and 2 CTAs of 256 threads fit an SM at 128 registers (P = 6: one CTA
+// per SM, pair_min_ctas).
 //
 // Consumer warp w owns rows 4w .. 4w+3 of the chunk and lane l the columns
 // l, l+32, l+64, l+96 of the block. B gives a lane its four rows of column j
@@ -263,6 +264,7 @@ struct PairMathF32 {
     using X = float;     // location element in shared memory
     using S = float;     // delta element
     using Part = float;  // row and column partials
+    static constexpr bool kXJEveryUnit = false;  // x_J is copied with the first unit of each block only
     static constexpr int kFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
     struct Cols {        // one column block: negated (x_j, x_j) packs and the column sums
         f2 nxj[4][P];
@@ -334,19 +336,20 @@ struct PairMathF32 {
 };
 
 // FP32 policy for larger P (5, 6): a pack is two columns of one row, so a lane
-// keeps only its column sums and x_j (two column-pair packs x P) for the block
-// and one row's x_i and row sums at a time. Columns (l, l+32) and (l+64, l+96)
-// form the two column pairs; B rows come as 128-bit loads of four rows each,
-// and a pack takes the same row from two of them.
+// keeps only its column sums (two column-pair packs x P) for the block and one
+// row's x_i and row sums at a time; x_J comes with every unit and the lane reads
+// its x_j pairs from shared memory. Columns (l, l+32) and (l+64, l+96) form the
+// two column pairs; B rows come as 128-bit loads of four rows each, and a pack
+// takes the same row from two of them.
 template <int P, bool TRUNC>
 struct PairMathF32Cols {
     using X = float;
     using S = float;
     using Part = float;
     static constexpr int kFoldUnits = 4;  // per half: 16 r^2 terms and 8 factors of 1/Phi per unit
+    static constexpr bool kXJEveryUnit = true;
     struct Cols {
-        f2 nxj[2][P];  // (-x_j, -x_j') of columns (l + 64 cp, l + 64 cp + 32)
-        f2 acc[2][P];
+        f2 acc[2][P];  // column sums of columns (l + 64 cp, l + 64 cp + 32)
     };
     using Sums = typename PairMathF32<P, TRUNC>::Sums;
     PairConstsF32 k;
@@ -356,14 +359,11 @@ struct PairMathF32Cols {
             pk(-a.tp2, -a.tp2), pk(a.ts0, a.ts0), pk(a.ts1, a.ts1),         pk(a.ts2, a.ts2)} {}
 
     __device__ static void init(Sums& s) { PairMathF32<P, TRUNC>::init(s); }
-    __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
+    __device__ static void begin_block(Cols& cols, const X*, int) {
 #pragma unroll
         for (int cp = 0; cp < 2; ++cp)
 #pragma unroll
-            for (int q = 0; q < P; ++q) {
-                cols.nxj[cp][q] = pk(-sXJ[q * kPairCols + lane + 64 * cp], -sXJ[q * kPairCols + lane + 64 * cp + 32]);
-                cols.acc[cp][q] = pk(0.f, 0.f);
-            }
+            for (int q = 0; q < P; ++q) cols.acc[cp][q] = pk(0.f, 0.f);
     }
     template <bool MASKED>
     __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
@@ -386,6 +386,12 @@ struct PairMathF32Cols {
             const int i = i0 + r;
 #pragma unroll
             for (int cp = 0; cp < 2; ++cp) {
+                // this unit's x_J follows x_I in the stage
+                const float* sXJ = sXI + (P + 1) * kPairRows;
+                f2 nxj[P];
+#pragma unroll
+                for (int q = 0; q < P; ++q)
+                    nxj[q] = pk(-sXJ[q * kPairCols + lane + 64 * cp], -sXJ[q * kPairCols + lane + 64 * cp + 32]);
                 const float a0 = sA[(4 * warp + r) * kPairCols + lane + 64 * cp];
                 const float a1 = sA[(4 * warp + r) * kPairCols + lane + 64 * cp + 32];
                 const float4& b0 = b[2 * cp];
@@ -402,7 +408,7 @@ struct PairMathF32Cols {
                     vB0 = ok0 && (d0 == d0);
                     vB1 = ok1 && (d1 == d1);
                 }
-                pair_pack<P, TRUNC, MASKED>(xi, cols.nxj[cp], pk(a0, a1), pk(d0, d1), vA0, vA1, vB0, vB1, k, racc,
+                pair_pack<P, TRUNC, MASKED>(xi, nxj, pk(a0, a1), pk(d0, d1), vA0, vA1, vB0, vB1, k, racc,
                                             cols.acc[cp], s.r2, s.prod, prodm);
             }
 #pragma unroll
@@ -486,6 +492,7 @@ struct PairMathF64 {
     using X = double;
     using S = DeltaT;  // float (DELTA_F32 mode) or double (FP64 mode)
     using Part = double;
+    static constexpr bool kXJEveryUnit = false;
     static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
         double xj[4][P];
@@ -574,10 +581,36 @@ struct PairMathF64 {
     }
 };
 
+// Sums each of the KV values over the warp's lanes and stores total i at
+// out[i]: one transpose-reduce for KV <= 16, else chunks of 8 (fewer live
+// registers than one reduce padded to 32 values).
+template <int KV, typename T>
+__device__ __forceinline__ void flush_row_sums(T (&v)[KV], T* out, int lane) {
+    constexpr int CH = KV <= 16 ? KV : 8;
+#pragma unroll
+    for (int c0 = 0; c0 < KV; c0 += CH) {
+        T w[CH];
+#pragma unroll
+        for (int i = 0; i < CH; ++i) w[i] = c0 + i < KV ? v[c0 + i] : T(0);
+        using TS = TransposeShape<CH>;
+        warp_transpose_reduce<CH>(w, lane);
+        const int idx = lane >> TS::kLaneShift;
+        if ((lane & ((1 << TS::kLaneShift) - 1)) == 0 && idx < CH && c0 + idx < KV) out[c0 + idx] = w[0];
+    }
+}
+
 // --------------------------------------------------------------- the kernel
 
+// CTAs per SM the kernel is compiled for: two at 128 registers; P = 6 runs one
+// CTA per SM with up to 255 registers (at 128 it spills: 0.77 ms against 0.49 at
+// N = 20 000, P = 6).
+template <int P>
+constexpr int pair_min_ctas() {
+    return P <= 5 ? 2 : 1;
+}
+
 template <int P, bool TRUNC, class M>
-__global__ void __launch_bounds__(kPairThreads, 2)
+__global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>())
     pair_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
                 const __grid_constant__ CUtensorMap tmap_xi, const __grid_constant__ CUtensorMap tmap_xj,
                 const PairArgs a) {
@@ -640,7 +673,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
                 }
             }
             unsigned char* st = smem + stage * Shape::kStageBytes;
-            const bool new_j = pJ != pJ_loaded;
+            const bool new_j = M::kXJEveryUnit || pJ != pJ_loaded;
             const uint32_t bytes =
                 Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
             mbar_arrive_expect_tx(&full[stage], bytes);
@@ -714,14 +747,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
             if (lane == 0) mbar_arrive(&empty[stage]);
 
             // row sums of this unit: rows 4w .. 4w+3, value index r * P + q
-            {
-                constexpr int KV = 4 * P;
-                using TS = TransposeShape<KV>;
-                warp_transpose_reduce<KV>(v, lane);
-                const int idx = lane >> TS::kLaneShift;
-                if ((lane & ((1 << TS::kLaneShift) - 1)) == 0 && idx < KV)
-                    rowpart[((size_t)(u_begin + k) * kPairRows + 4 * warp) * P + idx] = v[0];
-            }
+            flush_row_sums<4 * P>(v, rowpart + ((size_t)(u_begin + k) * kPairRows + 4 * warp) * P, lane);
             M::after_unit(sums);
         }
         if (!alive) break;

