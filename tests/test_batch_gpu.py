@@ -222,6 +222,6 @@ def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
         assert b.tune(repetitions=3) >= 3
         for p in (2, 3, 6):
             sc, rw, ctas, grid = b.group_shape(p)
-            assert sc in (0, 1, 2) and rw in ((1, 2, 4) if p <= 4 else (1, 2)) and ctas in (1, 2) and grid >= 1
-            assert sc != 2 or (p <= 6 and rw == 4)
+            assert sc in (0, 1, 2) and ctas in (1, 2) and grid >= 1
+            assert rw == 4 if sc == 2 else rw in ((1, 2, 4) if p <= 4 else (1, 2))
         _check(b, problems)
