@@ -25,8 +25,8 @@
 //   x_J = the same over J's 128 columns, with the first unit of each J
 // into a ring of PairShape::kStages stages (mbarrier full/empty pairs). Lane 0
 // of warp 0 issues the copies between its own units, so all 8 warps of a CTA
-// compute and 2 CTAs of 256 threads fit an SM at 128 registers (P = 6: one CTA
-// per SM, pair_min_ctas).
+// compute and 2 CTAs of 256 threads fit an SM at 128 registers (P = 4, 6: one
+// CTA per SM, pair_min_ctas).
 //
 // Consumer warp w owns rows 4w .. 4w+3 of the chunk and lane l the columns
 // l, l+32, l+64, l+96 of the block. B gives a lane its four rows of column j
@@ -601,12 +601,12 @@ __device__ __forceinline__ void flush_row_sums(T (&v)[KV], T* out, int lane) {
 
 // --------------------------------------------------------------- the kernel
 
-// CTAs per SM the kernel is compiled for: two at 128 registers; P = 6 runs one
-// CTA per SM with up to 255 registers (at 128 it spills: 0.77 ms against 0.49 at
-// N = 20 000, P = 6).
+// CTAs per SM the kernel is compiled for: two at 128 registers, or one with up
+// to 255 where 128 spills. Measured at N = 20 000 (FP32, truncated; two / one):
+// P = 3 0.336 / 0.385 ms, P = 4 0.429 / 0.400, P = 5 0.423 / 0.449, P = 6 0.77 / 0.49.
 template <int P>
 constexpr int pair_min_ctas() {
-    return P <= 5 ? 2 : 1;
+    return (P == 4 || P == 6) ? 1 : 2;
 }
 
 template <int P, bool TRUNC, class M>
