@@ -151,6 +151,13 @@ int mdsx_last_launch_count(mdsx_engine* engine, int* out);
 int mdsx_set_sweep_schedule(mdsx_engine* engine, int schedule);
 int mdsx_get_sweep_schedule(mdsx_engine* engine, int* out);
 
+/* Self-test of the bounded device waits (no counterpart in the reference): a
+ * one-thread kernel on `device` (< 0: current) waits on a barrier that never
+ * completes, gives up after limit_seconds (0 < limit <= 10) and records the
+ * timeout. Returns MDSX_ETIMEOUT with *device_code = 1 when the wait gave up as
+ * designed (the context stays usable), MDSX_ECUDA otherwise. */
+int mdsx_selftest_bounded_wait(double limit_seconds, int device, int* device_code);
+
 /* ---- Learned gradient surrogate (no counterpart in the reference) ----
  * g_i ~= s * sum_k alpha_ik (x_i - x_{l_k}) over K landmark locations (a
  * seeded random subset), alpha_i = MLP(features_i) with rotation-invariant

@@ -36,6 +36,7 @@
 #include "../../include/mdsx.h"
 #include "batch_sweep.h"
 #include "normal_rational.h"
+#include "pair_plan.h"
 #include "sweep.h"
 
 namespace mdsx {
@@ -338,66 +339,23 @@ void set_precision_constants(D& d, double tau) {
 // tables of its column blocks, its partial buffers, tensor maps and a PairArgs
 // descriptor.
 int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
-    using mdsx::pair_unit_cost;
-    using mdsx::pair_units_before;
-    struct Geo {
-        int nb, nc;
-        long long units, begin;
-    };
-    std::vector<Geo> geo;
-    long long U = 0;
-    double total = 0.0;
-    for (int k : g.members) {
-        const BatchInst& in = b->inst[k];
-        Geo q;
-        q.nb = (in.n + mdsx::kPairCols - 1) / mdsx::kPairCols;
-        q.nc = (in.n + mdsx::kPairRows - 1) / mdsx::kPairRows;
-        q.units = pair_units_before(q.nb, q.nc);
-        q.begin = U;
-        U += q.units;
-        for (int J = 0; J < q.nb; ++J)
-            for (int I = 4 * J; I < q.nc; ++I) total += pair_unit_cost(I, J);
-        geo.push_back(q);
-    }
-    g.n_units = U;
-    const int G = (int)std::min<long long>(U, (long long)b->sm_count * g.ctas_per_sm);
-    g.grid = G;
-    // cost-balanced CTA ranges, strictly increasing with room for the ranges after each
-    std::vector<long long> begin(G + 1);
-    {
-        int c = 1;
-        double cum = 0.0;
-        long long u = 0;
-        begin[0] = 0;
-        for (size_t m = 0; m < geo.size() && c < G; ++m)
-            for (int J = 0; J < geo[m].nb && c < G; ++J)
-                for (int I = 4 * J; I < geo[m].nc && c < G; ++I, ++u) {
-                    while (c < G && cum >= total * c / G) begin[c++] = u;
-                    cum += pair_unit_cost(I, J);
-                }
-        while (c < G) begin[c++] = U;
-        begin[G] = U;
-        for (int k = 1; k < G; ++k) begin[k] = std::min(std::max(begin[k], begin[k - 1] + 1), U - (G - k));
-    }
-    auto cta_of = [&](long long u) {  // CTA whose range holds global unit u
-        return (int)(std::upper_bound(begin.begin(), begin.end(), u) - begin.begin()) - 1;
-    };
+    std::vector<int> ns;
+    for (int k : g.members) ns.push_back(b->inst[k].n);
+    const mdsx::PairPlan plan = mdsx::pair_plan(ns, (long long)b->sm_count * g.ctas_per_sm);
+    g.n_units = plan.units;
+    g.grid = plan.grid;
+    const int G = plan.grid;
+    const std::vector<long long>& begin = plan.cta_begin;
     cudaStream_t st = b->stream;
     int finish = 0;
     for (size_t m = 0; m < g.members.size(); ++m) {
         BatchInst& in = b->inst[g.members[m]];
-        const Geo& q = geo[m];
-        std::vector<int> jfirst(q.nb), jslots(q.nb);
-        int max_slots = 1;
-        for (int J = 0; J < q.nb; ++J) {
-            const long long u0 = q.begin + pair_units_before(J, q.nc);
-            const long long u1 = u0 + (q.nc - 4 * J) - 1;
-            jfirst[J] = cta_of(u0);
-            jslots[J] = cta_of(u1) - jfirst[J] + 1;
-            max_slots = std::max(max_slots, jslots[J]);
-        }
-        const int first_cta = cta_of(q.begin);
-        const int islots = cta_of(q.begin + q.units - 1) - first_cta + 1;
+        const mdsx::PairInstancePlan& q = plan.inst[m];
+        const std::vector<int>& jfirst = q.j_first;
+        const std::vector<int>& jslots = q.j_slots;
+        const int max_slots = q.max_slots;
+        const int first_cta = q.first_cta;
+        const int islots = q.ctas;
         BCUDA(b, cudaMalloc(&in.d_prow, (size_t)q.units * mdsx::kPairRows * g.p * sizeof(float)));
         BCUDA(b, cudaMalloc(&in.d_pcol,
                             (size_t)q.nb * max_slots * mdsx::kPairWarps * g.p * mdsx::kPairCols * sizeof(float)));
@@ -431,7 +389,7 @@ int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
         a.lpart = in.d_plp;
         a.j_first_cta = in.d_pjfirst;
         a.j_slots = in.d_pjslots;
-        d.unit_begin = q.begin;
+        d.unit_begin = q.unit_begin;
         d.first_cta = first_cta;
         d.finish_begin = finish;
         finish += q.nc + 1;

@@ -28,6 +28,7 @@
 #include "../../include/mdsx.h"
 #include "normal_rational.h"
 #include "pair_kernel.cuh"
+#include "pair_plan.h"
 #include "engine_internal.h"
 #include "sweep.h"
 
@@ -121,43 +122,14 @@ int plan_pairs(mdsx_engine* e) {
     e->pair_nb = (e->n + mdsx::kPairCols - 1) / mdsx::kPairCols;
     e->pair_nc = (e->n + mdsx::kPairRows - 1) / mdsx::kPairRows;
     e->pair_units = mdsx::pair_units_before(e->pair_nb, e->pair_nc);
-    e->pair_grid = (int)std::min<long long>(e->pair_units, (long long)e->sm_count * ctas);
-    // Cost-balanced split: CTA c starts at the first unit whose cumulative modelled
-    // cost reaches c / G of the total; every range keeps at least one unit.
-    const int G = e->pair_grid;
-    const long long U = e->pair_units;
-    double total = 0.0;
-    for (int J = 0; J < e->pair_nb; ++J)
-        for (int I = 4 * J; I < e->pair_nc; ++I) total += mdsx::pair_unit_cost(I, J);
-    std::vector<long long> begin(G + 1);
-    {
-        int c = 1;
-        double cum = 0.0;
-        long long u = 0;
-        begin[0] = 0;
-        for (int J = 0; J < e->pair_nb && c < G; ++J)
-            for (int I = 4 * J; I < e->pair_nc && c < G; ++I, ++u) {
-                while (c < G && cum >= total * c / G) begin[c++] = u;
-                cum += mdsx::pair_unit_cost(I, J);
-            }
-        while (c < G) begin[c++] = U;
-        begin[G] = U;
-        // strictly increasing with room for the ranges after it (G <= U)
-        for (int k = 1; k < G; ++k)
-            begin[k] = std::min(std::max(begin[k], begin[k - 1] + 1), U - (G - k));
-    }
-    std::vector<int> jfirst(e->pair_nb), jslots(e->pair_nb);
-    e->pair_max_slots = 1;
-    for (int J = 0, c = 0; J < e->pair_nb; ++J) {
-        const long long u0 = mdsx::pair_units_before(J, e->pair_nc);
-        const long long u1 = u0 + (e->pair_nc - 4 * J) - 1;
-        while (begin[c + 1] <= u0) ++c;
-        int c1 = c;
-        while (begin[c1 + 1] <= u1) ++c1;
-        jfirst[J] = c;
-        jslots[J] = c1 - c + 1;
-        e->pair_max_slots = std::max(e->pair_max_slots, jslots[J]);
-    }
+    const mdsx::PairPlan plan = mdsx::pair_plan({e->n}, (long long)e->sm_count * ctas);
+    const mdsx::PairInstancePlan& q = plan.inst[0];
+    e->pair_grid = plan.grid;
+    e->pair_max_slots = q.max_slots;
+    const int G = plan.grid;
+    const std::vector<long long>& begin = plan.cta_begin;
+    const std::vector<int>& jfirst = q.j_first;
+    const std::vector<int>& jslots = q.j_slots;
     MDSX_CUDA(e, cudaMalloc(&e->d_pair_begin, (size_t)(G + 1) * sizeof(long long)));
     MDSX_CUDA(e, cudaMalloc(&e->d_pair_jfirst, (size_t)e->pair_nb * sizeof(int)));
     MDSX_CUDA(e, cudaMalloc(&e->d_pair_jslots, (size_t)e->pair_nb * sizeof(int)));

@@ -58,16 +58,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Waits for phase `parity` of `bar` to complete. Returns false (after writing
-// `code` into *err) when kWaitLimitNs pass first, or when another thread of the
+// `code` into *err) when limit_ns pass first, or when another thread of the
 // grid has already reported an error.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code,
+                                                  uint64_t limit_ns = kWaitLimitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t start = global_timer_ns();
     for (uint32_t spin = 1;; ++spin) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((spin & 255u) == 0) {
             if (*reinterpret_cast<volatile int*>(err) != kDevOk) return false;
-            if (global_timer_ns() - start > kWaitLimitNs) {
+            if (global_timer_ns() - start > limit_ns) {
                 atomicCAS(err, kDevOk, code);
                 return false;
             }

@@ -406,3 +406,23 @@ def test_full_size_n20000(mode, n20000):
     e.close()
     assert rel(s, s_ref) < tol_s
     assert grad_rel(g, g_ref) < tol_g
+
+
+# ------------------------------------------------- bounded waits (failure path)
+
+def test_bounded_wait_gives_up_and_context_stays_usable():
+    """A kernel waiting on a barrier that never completes gives up after its
+    limit, records the timeout code and returns; the GPU context stays usable
+    (an engine evaluates correctly afterwards). The wait ends by its time limit:
+    no fault or trap is involved."""
+    import ctypes
+    from massivemds_gb300 import _lib
+    lib = _lib.load()
+    code = ctypes.c_int(-1)
+    status = lib.mdsx_selftest_bounded_wait(ctypes.c_double(0.2), -1, ctypes.byref(code))
+    assert status == 4 and code.value == 1  # MDSX_ETIMEOUT, device code: consumer wait timed out
+    n, p, tau = 200, 2, 1.5
+    delta, x = _inputs(n, p, seed=50)
+    e = make_engine(n, p, True, "f32", delta, x, tau)
+    assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau)) < TOL_F32
+    e.close()
