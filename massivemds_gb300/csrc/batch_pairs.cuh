@@ -166,68 +166,24 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>()) batch_pair_k
             const int k_end = (int)((u_end < j_end ? u_end : j_end) - u_begin);
             const int slot = (int)blockIdx.x - a.j_first_cta[J];
             int I = 4 * J + (int)(u_begin + k - in.unit_begin - before);
-            const int j0 = J * kPairCols;
-
             typename M::Cols cols;
             bool j_masked = false;
-
             for (const int k_first = k; k < k_end; ++k, ++I) {
                 if (issuer) top_up(k);
-                const int stage = k % S;
-                if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / S) & 1u, ba.err, kDevTimeoutFull)) {
+                if (!pair_consume_unit<P, M, Shape>(math, sums, cols, j_masked, k == k_first, smem, full, empty, k, I,
+                                                    J, a.n, lane, warp, ba.err,
+                                                    rowpart + (size_t)(u_begin + k - in.unit_begin) * kPairRows * P)) {
                     alive = false;
                     break;
                 }
-                const unsigned char* st = smem + stage * Shape::kStageBytes;
-                const float* sB = reinterpret_cast<const float*>(st);
-                const float* sA = reinterpret_cast<const float*>(st + Shape::kBBytes);
-                const float* sXI = reinterpret_cast<const float*>(st + Shape::kXIOffset);
-                if (k == k_first) {
-                    const float* sXJ = reinterpret_cast<const float*>(st + Shape::kXJOffset);
-                    M::begin_block(cols, sXJ, lane);
-                    bool bad = false;
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) bad |= sXJ[P * kPairCols + lane + 32 * c] != 0.f;
-                    j_masked = __any_sync(0xffffffffu, bad);
-                }
-                const float* fl = sXI + P * kPairRows + 4 * warp;
-                const bool masked =
-                    j_masked || (I < 4 * J + 4) || fl[0] != 0.f || fl[1] != 0.f || fl[2] != 0.f || fl[3] != 0.f;
-                const int i0 = I * kPairRows + 4 * warp;
-
-                float v[4 * P];
-                if (masked)
-                    math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
-                else
-                    math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&empty[stage]);
-                flush_row_sums<4 * P>(v, rowpart + ((size_t)(u_begin + k - in.unit_begin) * kPairRows + 4 * warp) * P,
-                                      lane);
-                M::after_unit(sums);
             }
             if (!alive) break;
-#pragma unroll
-            for (int q = 0; q < P; ++q)
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    colpart[(((size_t)J * a.max_slots + slot) * kPairWarps + warp) * (P * kPairCols) + q * kPairCols +
-                            lane + 32 * c] = M::col_value(cols, c, q);
+            pair_flush_cols<P, M>(cols, colpart + (size_t)J * a.max_slots * kPairWarps * (P * kPairCols), slot, warp,
+                                  lane);
         }
         if (!alive) break;
         // this CTA's likelihood sums of the instance, per warp
-        double r2_sum, lsum;
-        M::result(sums, r2_sum, lsum);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
-            lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
-        }
-        if (lane == 0) {
-            const size_t e = ((size_t)(blockIdx.x - in.first_cta) * kPairWarps + warp) * 2;
-            a.lpart[e] = r2_sum;
-            a.lpart[e + 1] = lsum;
-        }
+        pair_flush_likelihood<M>(sums, a.lpart + ((size_t)(blockIdx.x - in.first_cta) * kPairWarps + warp) * 2, lane);
     }
 
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

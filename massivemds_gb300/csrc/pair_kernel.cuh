@@ -153,7 +153,7 @@ __device__ __forceinline__ void pair_pack(const f2 (&xi)[P], const f2 (&nxj)[P],
     f2 dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = fadd2(xi[q], nxj[q]);  // x_i - x_j
-    f2 d2 = fmul2(dx[0], dx[0]);
+    f2 d2 = ffma2(dx[0], dx[0], k.tiny);  // coincident points: d ~ 1e-15, not NaN (PairConstsF32)
 #pragma unroll
     for (int q = 1; q < P; ++q) d2 = ffma2(dx[q], dx[q], d2);
     const f2 rs = rsqrt2(d2);
@@ -455,7 +455,9 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
     for (int q = 1; q < P; ++q) d2 = fma(dx[q], dx[q], d2);
     if (MASKED && !(vA || vB)) return;
     const double rs = rsqrt(d2);
-    const double d = d2 * rs;
+    // coincident points (d2 = 0, i != j): d = 0 as the reference's sqrt gives, so the
+    // likelihood term is finite; rs = inf makes their gradient terms NaN, as the reference's
+    const double d = d2 > 0.0 ? d2 * rs : 0.0;
     const double resA = dA - d, resB = dB - d;
     if (!MASKED || vA) r2 = fma(resA, resA, r2);
     if (!MASKED || vB) r2 = fma(resB, resB, r2);
@@ -599,6 +601,80 @@ __device__ __forceinline__ void flush_row_sums(T (&v)[KV], T* out, int lane) {
     }
 }
 
+// One unit of the consumer loop (shared by pair_kernel and batch_pair_kernel):
+// waits (bounded) for the unit's stage, takes x_J and the column flags when the
+// unit starts a column block, runs the math policy on the masked or fast path,
+// releases the stage and writes the unit's row sums to `rowpart_unit` (the
+// unit's [32][P] rows). Returns false if the wait gave up.
+template <int P, class M, class Shape>
+__device__ __forceinline__ bool pair_consume_unit(const M& math, typename M::Sums& sums, typename M::Cols& cols,
+                                                  bool& j_masked, bool block_start, const unsigned char* smem,
+                                                  uint64_t* full, uint64_t* empty, int k, int I, int J, int n,
+                                                  int lane, int warp, int* err, typename M::Part* rowpart_unit) {
+    using X = typename M::X;
+    using DS = typename M::S;
+    constexpr int S = Shape::kStages;
+    const int stage = k % S;
+    if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / S) & 1u, err, kDevTimeoutFull)) return false;
+    const unsigned char* st = smem + stage * Shape::kStageBytes;
+    const DS* sB = reinterpret_cast<const DS*>(st);
+    const DS* sA = reinterpret_cast<const DS*>(st + Shape::kBBytes);
+    const X* sXI = reinterpret_cast<const X*>(st + Shape::kXIOffset);
+    if (block_start) {
+        // x_J arrived with this unit: the block's x_j and its column flags
+        const X* sXJ = reinterpret_cast<const X*>(st + Shape::kXJOffset);
+        M::begin_block(cols, sXJ, lane);
+        bool bad = false;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) bad |= sXJ[P * kPairCols + lane + 32 * c] != X(0);
+        j_masked = __any_sync(0xffffffffu, bad);
+    }
+    const X* fl = sXI + P * kPairRows + 4 * warp;
+    const bool masked = j_masked || (I < 4 * J + 4) || fl[0] != X(0) || fl[1] != X(0) || fl[2] != X(0) || fl[3] != X(0);
+    const int i0 = I * kPairRows + 4 * warp;
+    const int j0 = J * kPairCols;
+    typename M::Part v[4 * P];
+    if (masked)
+        math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
+    else
+        math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[stage]);
+    // row sums of this unit: rows 4w .. 4w+3, value index r * P + q
+    flush_row_sums<4 * P>(v, rowpart_unit + (size_t)(4 * warp) * P, lane);
+    M::after_unit(sums);
+    return true;
+}
+
+// Column sums of one column block from this warp: colpart_block = the block's
+// [slots][8 warps][P][128] partials, slot = this CTA's slot of the block.
+template <int P, class M>
+__device__ __forceinline__ void pair_flush_cols(const typename M::Cols& cols, typename M::Part* colpart_block,
+                                                int slot, int warp, int lane) {
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            colpart_block[((size_t)slot * kPairWarps + warp) * (P * kPairCols) + q * kPairCols + lane + 32 * c] =
+                M::col_value(cols, c, q);
+}
+
+// This warp's likelihood sums (r^2, log Phi) reduced over its lanes, written by lane 0 at lpart_entry[0..1].
+template <class M>
+__device__ __forceinline__ void pair_flush_likelihood(typename M::Sums& sums, double* lpart_entry, int lane) {
+    double r2_sum, lsum;
+    M::result(sums, r2_sum, lsum);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
+    }
+    if (lane == 0) {
+        lpart_entry[0] = r2_sum;
+        lpart_entry[1] = lsum;
+    }
+}
+
 // --------------------------------------------------------------- the kernel
 
 // CTAs per SM the kernel is compiled for: two at 128 registers, or one with up
@@ -708,56 +784,20 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>())
         const int k_end = (int)((u_end < j_end ? u_end : j_end) - u_begin);
         const int slot = (int)blockIdx.x - a.j_first_cta[J];
         int I = 4 * J + (int)(u_begin + k - before);
-        const int j0 = J * kPairCols;
-
         typename M::Cols cols;
         bool j_masked = false;
-
         for (const int k_first = k; k < k_end; ++k, ++I) {
             if (issuer) top_up(k);
-            const int stage = k % S;
-            if (!mbar_wait_bounded(&full[stage], (uint32_t)(k / S) & 1u, a.err, kDevTimeoutFull)) {
+            if (!pair_consume_unit<P, M, Shape>(math, sums, cols, j_masked, k == k_first, smem, full, empty, k, I, J,
+                                                a.n, lane, warp, a.err,
+                                                rowpart + (size_t)(u_begin + k) * kPairRows * P)) {
                 alive = false;
                 break;
             }
-            const unsigned char* st = smem + stage * Shape::kStageBytes;
-            const DS* sB = reinterpret_cast<const DS*>(st);
-            const DS* sA = reinterpret_cast<const DS*>(st + Shape::kBBytes);
-            const X* sXI = reinterpret_cast<const X*>(st + Shape::kXIOffset);
-            if (k == k_first) {
-                // x_J arrived with this unit: the block's x_j and its column flags
-                const X* sXJ = reinterpret_cast<const X*>(st + Shape::kXJOffset);
-                M::begin_block(cols, sXJ, lane);
-                bool bad = false;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) bad |= sXJ[P * kPairCols + lane + 32 * c] != X(0);
-                j_masked = __any_sync(0xffffffffu, bad);
-            }
-            const X* fl = sXI + P * kPairRows + 4 * warp;
-            const bool masked =
-                j_masked || (I < 4 * J + 4) || fl[0] != X(0) || fl[1] != X(0) || fl[2] != X(0) || fl[3] != X(0);
-            const int i0 = I * kPairRows + 4 * warp;
-
-            Part v[4 * P];
-            if (masked)
-                math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
-            else
-                math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, a.n, lane, warp, v);
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[stage]);
-
-            // row sums of this unit: rows 4w .. 4w+3, value index r * P + q
-            flush_row_sums<4 * P>(v, rowpart + ((size_t)(u_begin + k) * kPairRows + 4 * warp) * P, lane);
-            M::after_unit(sums);
         }
         if (!alive) break;
-        // column sums of block J from this CTA: [J][slot][warp][q][128]
-#pragma unroll
-        for (int q = 0; q < P; ++q)
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-                colpart[(((size_t)J * a.max_slots + slot) * kPairWarps + warp) * (P * kPairCols) + q * kPairCols + lane +
-                        32 * c] = M::col_value(cols, c, q);
+        pair_flush_cols<P, M>(cols, colpart + (size_t)J * a.max_slots * kPairWarps * (P * kPairCols), slot, warp,
+                              lane);
     }
 
     // The finish kernel may be scheduled now; it waits for this grid to complete.
@@ -768,17 +808,7 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>())
     }
     if (!alive) return;
 
-    double r2_sum, lsum;
-    M::result(sums, r2_sum, lsum);
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        r2_sum += __shfl_xor_sync(0xffffffffu, r2_sum, off);
-        lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
-    }
-    if (lane == 0) {
-        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 0] = r2_sum;
-        a.lpart[((size_t)blockIdx.x * kPairWarps + warp) * 2 + 1] = lsum;
-    }
+    pair_flush_likelihood<M>(sums, a.lpart + ((size_t)blockIdx.x * kPairWarps + warp) * 2, lane);
 }
 
 // Sum of K values (K a power of two) as a fixed pairwise tree in their own

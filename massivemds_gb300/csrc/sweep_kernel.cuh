@@ -170,8 +170,12 @@ __device__ __forceinline__ float sum2(f2 x) {
 // Pair constants in d-space, each duplicated into a pack:
 //   E'    = 2^(d^2 k_e + log2_k2) = exp(-tau d^2 / 2) / sqrt(2 pi tau)
 //   1/Phi = S(d) / A,  A = S(d) - E' P(d),  S monic cubic (ts*), P quadratic (-P = ntp*)
+//   tiny  = 1e-30, the start of the d^2 sum: d^2 is unchanged above ~1e-23, and
+//           coincident points (d^2 = 0, i != j) get d ~ 1e-15 instead of 0 * inf =
+//           NaN, so their likelihood term is the reference's (d = 0) and finite.
 struct PairConstsF32 {
     f2 m1, k_e, log2_k2, ntp0, ntp1, ntp2, ts0, ts1, ts2;
+    f2 tiny{0x0DA242600DA24260ull};  // (1e-30f, 1e-30f)
 };
 
 // Two ordered pairs (i, j), (i, j+1) in packed FP32. With r = delta - d,
@@ -185,7 +189,7 @@ __device__ __forceinline__ void pair2_f32(const f2 (&xi)[P], const f2 (&xj)[P], 
     f2 dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = ffma2(xj[q], k.m1, xi[q]);  // x_i - x_j
-    f2 d2 = fmul2(dx[0], dx[0]);
+    f2 d2 = ffma2(dx[0], dx[0], k.tiny);
 #pragma unroll
     for (int q = 1; q < P; ++q) d2 = ffma2(dx[q], dx[q], d2);
     const f2 rs = rsqrt2(d2);

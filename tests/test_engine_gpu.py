@@ -426,3 +426,31 @@ def test_bounded_wait_gives_up_and_context_stays_usable():
     e = make_engine(n, p, True, "f32", delta, x, tau)
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau)) < TOL_F32
     e.close()
+
+
+def test_coincident_points():
+    """Two distinct rows at the same location (d = 0 for a non-missing pair): the
+    reference takes d = sqrt(0) = 0, so the likelihood term is finite, and
+    divides by d in the gradient, so the two rows' gradients are NaN. FP64 modes
+    reproduce both; FP32 modes reproduce the likelihood and keep the two rows'
+    gradients finite (d^2 starts from 1e-30); every other row matches."""
+    n, p, tau = 200, 2, 1.3
+    delta, x = _inputs(n, p, seed=60)
+    x[7] = x[3]
+    for mode in ("f64rows", "f64pairs", "f64s32pairs", "f32rows", "f32pairs"):
+        tol_s, tol_g = tolerances(mode)
+        od = oracle_delta(delta, mode)
+        s_ref = oracle.sum_of_increments(od, x, tau)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            g_ref = oracle.gradient(od, x, tau)
+        assert np.isfinite(s_ref) and np.isnan(g_ref[[3, 7]]).all()
+        e = make_engine(n, p, True, mode, delta, x, tau)
+        s, g = e.getSumOfIncrements(), np.asarray(e.getLogLikelihoodGradient()).reshape(n, p)
+        e.close()
+        assert np.isfinite(s) and rel(s, s_ref) < tol_s, mode
+        rest = np.setdiff1d(np.arange(n), [3, 7])
+        assert grad_rel(g[rest], g_ref[rest]) < tol_g, mode
+        if mode.startswith("f64"):
+            assert np.isnan(g[[3, 7]]).all(), mode
+        else:
+            assert np.isfinite(g[[3, 7]]).all(), mode
