@@ -15,6 +15,9 @@
 // device-to-host copy. Instance calls keep the reference's names and lazy
 // semantics: a getter evaluates the batch when any instance changed.
 //
+// Location updates go to a pinned host copy per instance and reach the device
+// with the next evaluation, so a caller updating every instance pays no
+// synchronisation per call.
 // Shapes (schedule, rows per warp, CTAs per SM) come from an autotuner that times
 // the candidates on the batch itself and caches the winner per (P, N-bucket,
 // truncation), in process and, when MDSX_TUNE_CACHE names a file, on disk.
@@ -153,6 +156,8 @@ struct BatchInst {
     float* d_x = nullptr;      // SoA [p + 1][x_ld]; row p: missing-row flags
     int x_ld = 0;
     double* d_xin = nullptr;   // row-major [n][p] staging
+    double* h_x = nullptr;     // pinned host copy of the locations, row-major [n][p]
+    bool x_dirty = false;      // h_x changed since the last upload
     // plan-dependent
     int* d_row_nan = nullptr;
     int rows_padded = 0, n_row_blocks = 0;
@@ -211,6 +216,8 @@ struct mdsx_batch {
     int* d_err = nullptr;
     double* h_results = nullptr;   // pinned: sums [count][4], then gradients
     long long grad_total = 0;
+    cudaEvent_t uploaded = nullptr;  // recorded after the location uploads of an evaluation
+    bool upload_pending = false;     // an upload from the pinned copies may still be in flight
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<cudaStream_t> aux;     // one branch stream per dimension group (graph capture)
@@ -677,6 +684,26 @@ int enqueue_groups(mdsx_batch* b) {
     return MDSX_OK;
 }
 
+// Uploads the locations of every instance updated since the last upload (one
+// copy from its pinned host copy and one layout conversion each) on the batch
+// stream, and records `uploaded` behind them.
+int flush_uploads(mdsx_batch* b) {
+    bool any = false;
+    for (auto& in : b->inst) {
+        if (!in.x_dirty) continue;
+        BCUDA(b, cudaMemcpyAsync(in.d_xin, in.h_x, (size_t)in.n * in.p * sizeof(double), cudaMemcpyHostToDevice,
+                                 b->stream));
+        BCUDA(b, mdsx::convert_locations(in.d_xin, in.n, in.p, in.d_x, in.x_ld, true, b->stream));
+        in.x_dirty = false;
+        any = true;
+    }
+    if (any) {
+        BCUDA(b, cudaEventRecord(b->uploaded, b->stream));
+        b->upload_pending = true;
+    }
+    return MDSX_OK;
+}
+
 // Enqueues one evaluation of every instance (graph launch); no synchronisation.
 int enqueue_evaluation(mdsx_batch* b) {
     if (!b->planned) {
@@ -685,6 +712,10 @@ int enqueue_evaluation(mdsx_batch* b) {
     }
     if (b->desc_dirty) {
         int rc = upload_descriptors(b);
+        if (rc) return rc;
+    }
+    {
+        int rc = flush_uploads(b);
         if (rc) return rc;
     }
     if (b->graph_dirty) {
@@ -758,8 +789,10 @@ int mdsx_batch_create(long flags, int device, mdsx_batch** out) {
     b->trunc = (flags & MDSX_FLAG_LEFT_TRUNCATION) != 0;
     if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess || cudaMemset(b->d_err, 0, sizeof(int)) != cudaSuccess) {
         if (b->stream) cudaStreamDestroy(b->stream);
+        if (b->uploaded) cudaEventDestroy(b->uploaded);
         cudaFree(b->d_err);
         delete b;
         return MDSX_ECUDA;
@@ -777,7 +810,9 @@ void mdsx_batch_destroy(mdsx_batch* b) {
         cudaFree(in.d_delta);
         cudaFree(in.d_x);
         cudaFree(in.d_xin);
+        if (in.h_x) cudaFreeHost(in.h_x);
     }
+    if (b->uploaded) cudaEventDestroy(b->uploaded);
     cudaFree(b->d_err);
     for (cudaStream_t st : b->aux) cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->aux_ev) cudaEventDestroy(ev);
@@ -805,12 +840,15 @@ int mdsx_batch_add_instance(mdsx_batch* b, int embedding_dimension, int location
     const size_t xb = (size_t)(in.p + 1) * in.x_ld * sizeof(float);  // row P: missing-row flags
     if (cudaMalloc(&in.d_delta, (size_t)in.n * in.ld * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&in.d_x, xb) != cudaSuccess ||
-        cudaMalloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&in.h_x, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
         cudaFree(in.d_delta);
         cudaFree(in.d_x);
         cudaFree(in.d_xin);
+        if (in.h_x) cudaFreeHost(in.h_x);
         return bfail(b, MDSX_ENOMEM, "instance allocation failed");
     }
+    std::memset(in.h_x, 0, (size_t)in.n * in.p * sizeof(double));
     BCUDA(b, cudaMemsetAsync(in.d_x, 0, xb, b->stream));
     BCUDA(b, cudaStreamSynchronize(b->stream));
     *instance = (int)b->inst.size();
@@ -885,20 +923,21 @@ int mdsx_batch_update_locations(mdsx_batch* b, int k, int index, const double* l
     if (rc) return rc;
     BatchInst& in = b->inst[k];
     if (!locations) return bfail(b, MDSX_EINVAL, "locations is NULL");
-    Guard guard(b->device);
     if (index == -1) {
         if (length != (size_t)in.n * in.p) return bfail(b, MDSX_EINVAL, "locations must hold N*P values");
-        BCUDA(b, cudaMemcpyAsync(in.d_xin, locations, length * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-        BCUDA(b, mdsx::convert_locations(in.d_xin, in.n, in.p, in.d_x, in.x_ld, true, b->stream));
-    } else {
-        if (index < 0 || index >= in.n || length != (size_t)in.p)
-            return bfail(b, MDSX_EINVAL, "location index out of range or length != P");
-        BCUDA(b, cudaMemcpyAsync(in.d_xin + (size_t)index * in.p, locations, length * sizeof(double),
-                                 cudaMemcpyHostToDevice, b->stream));
-        BCUDA(b, mdsx::set_one_location(in.d_xin + (size_t)index * in.p, index, in.p, in.d_x, in.x_ld, true,
-                                        b->stream));
+    } else if (index < 0 || index >= in.n || length != (size_t)in.p) {
+        return bfail(b, MDSX_EINVAL, "location index out of range or length != P");
     }
-    BCUDA(b, cudaStreamSynchronize(b->stream));  // the caller's buffer may change after return
+    // The values go to the instance's pinned host copy now and to the device with
+    // the next evaluation (one copy per changed instance, no synchronisation per
+    // call). Wait only if an upload from the pinned copies may still be reading them.
+    if (b->upload_pending) {
+        Guard guard(b->device);
+        BCUDA(b, cudaEventSynchronize(b->uploaded));
+        b->upload_pending = false;
+    }
+    std::memcpy(in.h_x + (index == -1 ? 0 : (size_t)index * in.p), locations, length * sizeof(double));
+    in.x_dirty = true;
     b->results_known = false;
     return MDSX_OK;
 }
@@ -1050,6 +1089,7 @@ int mdsx_batch_tune(mdsx_batch* b, int repetitions, int* candidates) {
     Guard guard(b->device);
     int rc = plan(b);
     if (rc) return rc;
+    if ((rc = flush_uploads(b))) return rc;  // time on the current locations
     struct Key {
         int p, trunc, bucket;
     };

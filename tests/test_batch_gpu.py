@@ -225,3 +225,29 @@ def test_tune_picks_a_built_shape_and_keeps_parity(tmp_path, monkeypatch):
             assert sc in (0, 1, 2) and ctas in (1, 2) and grid >= 1
             assert rw == 4 if sc == 2 else rw in ((1, 2, 4) if p <= 4 else (1, 2))
         _check(b, problems)
+
+
+def test_location_updates_right_after_an_asynchronous_evaluation():
+    """Location updates are staged in pinned host copies and uploaded with the
+    next evaluation; an update issued while the previous evaluation (and its
+    uploads) may still run must not change that evaluation's inputs, and the
+    next evaluation sees the new locations."""
+    torch = pytest.importorskip("torch")
+    problems = _problems([(900, 2), (700, 3), (500, 6), (1200, 2)], 31)
+    with Batch() as b:
+        _fill(b, problems)
+        total = sum(x.size for _, x, _ in problems)
+        d_sums = torch.zeros(4 * len(problems), dtype=torch.float64, device="cuda")
+        d_grads = torch.zeros(total, dtype=torch.float64, device="cuda")
+        b.evaluate_device(d_sums.data_ptr(), d_grads.data_ptr())  # enqueued, not synchronised
+        rng = np.random.default_rng(32)
+        new = []
+        for k, (delta, x, tau) in enumerate(problems):
+            x2 = x + 0.3 * rng.standard_normal(x.shape)
+            b.updateLocations(k, -1, x2)
+            new.append((delta, x2, tau))
+        torch.cuda.synchronize()
+        first = d_sums.cpu().numpy().reshape(-1, 4)[:, 2]
+        for k, (delta, x, tau) in enumerate(problems):
+            assert _rel(first[k], oracle.sum_of_increments(delta, x, tau)) < TOL, k
+        _check(b, new)
