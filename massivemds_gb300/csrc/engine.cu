@@ -283,46 +283,68 @@ SweepArgs make_args(mdsx_engine* e) {
     return a;
 }
 
+// Arguments of the unordered-pair sweep at the engine's current state.
+mdsx::PairArgs make_pair_args(mdsx_engine* e) {
+    const SweepArgs a = make_args(e);
+    mdsx::PairArgs pa{};
+    pa.n = e->n;
+    pa.nb = e->pair_nb;
+    pa.nc = e->pair_nc;
+    pa.grid = e->pair_grid;
+    pa.max_slots = e->pair_max_slots;
+    pa.truncation = a.truncation;
+    pa.n_units = e->pair_units;
+    pa.k_e = a.k_e;
+    pa.log2_k2 = a.log2_k2;
+    pa.tp0 = a.tp0;
+    pa.tp1 = a.tp1;
+    pa.tp2 = a.tp2;
+    pa.ts0 = a.ts0;
+    pa.ts1 = a.ts1;
+    pa.ts2 = a.ts2;
+    pa.tau = a.tau;
+    pa.sqrt_tau = a.sqrt_tau;
+    pa.rowpart = e->d_rowpart;
+    pa.colpart = e->d_colpart;
+    pa.lpart = e->d_plpart;
+    pa.cta_begin = e->d_pair_begin;
+    pa.j_first_cta = e->d_pair_jfirst;
+    pa.j_slots = e->d_pair_jslots;
+    pa.grad_out = a.grad_out;
+    pa.sums_out = a.sums_out;
+    pa.err = a.err;
+    return pa;
+}
+
 // Enqueues one fused sweep; does not synchronise.
 int enqueue_sweep(mdsx_engine* e) {
     if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
     if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
-    SweepArgs a = make_args(e);
     if (e->schedule == MDSX_SWEEP_PAIRS) {
-        mdsx::PairArgs pa{};
-        pa.n = e->n;
-        pa.nb = e->pair_nb;
-        pa.nc = e->pair_nc;
-        pa.grid = e->pair_grid;
-        pa.max_slots = e->pair_max_slots;
-        pa.truncation = a.truncation;
-        pa.n_units = e->pair_units;
-        pa.k_e = a.k_e;
-        pa.log2_k2 = a.log2_k2;
-        pa.tp0 = a.tp0;
-        pa.tp1 = a.tp1;
-        pa.tp2 = a.tp2;
-        pa.ts0 = a.ts0;
-        pa.ts1 = a.ts1;
-        pa.ts2 = a.ts2;
-        pa.tau = a.tau;
-        pa.sqrt_tau = a.sqrt_tau;
-        pa.rowpart = e->d_rowpart;
-        pa.colpart = e->d_colpart;
-        pa.lpart = e->d_plpart;
-        pa.cta_begin = e->d_pair_begin;
-        pa.j_first_cta = e->d_pair_jfirst;
-        pa.j_slots = e->d_pair_jslots;
-        pa.grad_out = a.grad_out;
-        pa.sums_out = a.sums_out;
-        pa.err = a.err;
+        const mdsx::PairArgs pa = make_pair_args(e);
         MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
         e->last_launches = 2;
         return MDSX_OK;
     }
+    SweepArgs a = make_args(e);
     MDSX_CUDA(e, mdsx::sweep_launch(e->mode, e->p, e->trunc, e->grid, e->tmap_delta, e->tmap_x[e->xcur], a,
                                     e->stream));
     e->last_launches = 1;
+    return MDSX_OK;
+}
+
+// Enqueues one fused sweep whose finish kernel also applies the leapfrog step
+// `lf` (unordered-pair schedule only; MDSX_EUNSUPPORTED otherwise, and the
+// caller runs its own kick/drift after enqueue_sweep).
+int enqueue_sweep_leapfrog(mdsx_engine* e, const mdsx::PairLeapfrog& lf) {
+    if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
+    if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
+    if (e->schedule != MDSX_SWEEP_PAIRS) return MDSX_EUNSUPPORTED;
+    mdsx::PairArgs pa = make_pair_args(e);
+    pa.leapfrog = 1;
+    pa.leap = lf;
+    MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
+    e->last_launches = 2;
     return MDSX_OK;
 }
 

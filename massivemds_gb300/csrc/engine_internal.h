@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/mdsx.h"
+#include "pair_kernel.cuh"
 #include "sweep.h"
 
 using mdsx::KernelShape;
@@ -97,6 +98,7 @@ struct DeviceGuard {
 
 // Enqueues one fused sweep at the current state (no synchronisation).
 int enqueue_sweep(mdsx_engine* e);
+int enqueue_sweep_leapfrog(mdsx_engine* e, const mdsx::PairLeapfrog& lf);
 // Runs a sweep and reads its sums back; sum and gradient become known.
 int sweep_and_read(mdsx_engine* e);
 // getSumOfIncrements() from the cached sums and the current precision.

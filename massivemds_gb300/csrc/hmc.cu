@@ -514,9 +514,28 @@ struct Chain {
             xfinal = cur;
             if (!rc) rc = internal::enqueue_sweep(e);  // exact potential at the proposal
         } else {
+            // with the unordered-pair schedule the sweep's finish kernel applies the
+            // kick/drift to the rows it completes (one launch less per step)
+            const bool fused = e->schedule == MDSX_SWEEP_PAIRS && p <= mdsx::kPairMaxP;
+            mdsx::PairLeapfrog lf{};
+            if (fused) {
+                lf.x = xp;
+                lf.mom = mom;
+                lf.soa = e->d_x[e->xcur];
+                lf.x_ld = e->x_ld;
+                lf.soa_f32 = e->x_f32 ? 1 : 0;
+                for (int r = 0; r < p; ++r)
+                    for (int q = 0; q < p; ++q) lf.lam[r * p + q] = lam.m[r * p + q];
+            }
             for (int k = 1; !rc && k <= L; ++k) {
-                rc = internal::enqueue_sweep(e);
-                if (!rc) rc = kick_drift(xp, e->d_grad[e->gcur], k < L ? coef + 2 : coef + 4);
+                const double* ck = k < L ? coef + 2 : coef + 4;
+                if (fused) {
+                    lf.coef = ck;
+                    rc = internal::enqueue_sweep_leapfrog(e, lf);
+                } else {
+                    rc = internal::enqueue_sweep(e);
+                    if (!rc) rc = kick_drift(xp, e->d_grad[e->gcur], ck);
+                }
             }
         }
         if (!rc) rc = reduce(0, mom, red_k);

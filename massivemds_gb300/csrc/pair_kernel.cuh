@@ -80,6 +80,19 @@ struct PairShape {
     static constexpr int kSmemBytes = kStages * kStageBytes + 2 * kStages * 8 + 1024;
 };
 
+// Optional leapfrog step fused into the finish kernel (the HMC driver): with
+// the gradient g of the sweep, p += a (g - x Lambda) and x += b p per location
+// (a = coef[0], b = coef[1]), x also written into the sweep's SoA location buffer.
+struct PairLeapfrog {
+    double* x;            // [N][P] positions
+    double* mom;          // [N][P] momenta
+    const double* coef;   // [2]: a, b (device memory: a captured graph follows step-size changes)
+    void* soa;            // SoA location buffer [P][x_ld] of the sweep (float or double)
+    int x_ld;
+    int soa_f32;
+    double lam[kPairMaxP * kPairMaxP];  // prior precision, row-major P x P
+};
+
 struct PairArgs {
     int n;               // locations N
     int nb;              // column blocks ceil(N / 128)
@@ -101,6 +114,8 @@ struct PairArgs {
     double* grad_out;  // [N][P]
     double* sums_out;  // [0] r^2, [1] logPhi over ordered non-missing pairs, [2] getSumOfIncrements()
     int* err;
+    int leapfrog;       // nonzero: the finish applies `leap` to its rows
+    PairLeapfrog leap;
 };
 
 // Units of the column blocks before J: sum over J' < J of (nc - 4 J').
@@ -922,12 +937,47 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
     }
     part[0][t] = acc;
     __syncthreads();
+    double grad_t = 0.0;
     if (t < FS::kOut) {
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < FS::kGroups; ++k) s += part[0][k * FS::kOut + t];
+        grad_t = a.tau * s;
         const int row = I * kPairRows + t / P;
-        if (row < a.n) a.grad_out[(size_t)I * FS::kOut + t] = a.tau * s;
+        if (row < a.n) a.grad_out[(size_t)I * FS::kOut + t] = grad_t;
+    }
+    if (!a.leapfrog) return;
+    // leapfrog for the chunk's rows: thread r < 32 takes row I * 32 + r
+    __syncthreads();  // every thread has read part[0]
+    if (t < FS::kOut) part[1][t] = grad_t;
+    __syncthreads();
+    const int row = I * kPairRows + t;
+    if (t < kPairRows && row < a.n) {
+        const PairLeapfrog& L = a.leap;
+        const double ca = L.coef[0], cb = L.coef[1];
+        double xi[P], pi[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            xi[q] = L.x[(size_t)row * P + q];
+            pi[q] = L.mom[(size_t)row * P + q];
+        }
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            double prior = 0.0;
+#pragma unroll
+            for (int r = 0; r < P; ++r) prior += xi[r] * L.lam[r * P + q];
+            pi[q] += ca * (part[1][t * P + q] - prior);
+        }
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            xi[q] += cb * pi[q];
+            L.mom[(size_t)row * P + q] = pi[q];
+            L.x[(size_t)row * P + q] = xi[q];
+            if (L.soa_f32)
+                static_cast<float*>(L.soa)[(size_t)q * L.x_ld + row] = (float)xi[q];
+            else
+                static_cast<double*>(L.soa)[(size_t)q * L.x_ld + row] = xi[q];
+        }
     }
 }
 

@@ -43,8 +43,11 @@ def test_one_trajectory_matches_restatement(use_graph):
     assert abs(res.column("log_likelihood")[0] - oracle.log_likelihood(s, n, tau)) < 1e-8 * abs(s)
 
 
-def test_second_iteration_uses_its_own_momentum():
-    n, p, tau, eps, steps, seed = 50, 3, 0.9, 0.003, 8, 5
+@pytest.mark.parametrize("p", [1, 3, 4])
+def test_second_iteration_uses_its_own_momentum(p):
+    # the truncated FP64 engine runs the unordered-pair sweep for P <= 4, whose
+    # finish kernel applies the kick/drift: P = 4 is its widest instance
+    n, tau, eps, steps, seed = 50, 0.9, 0.003, 8, 5
     delta, x0 = _problem(n, p, 6)
     e = _engine(delta, p, tau, 0)
     res = hmc(e, x0, iterations=2, leapfrog_steps=steps, step_size=eps, seed=seed)
@@ -58,8 +61,10 @@ def test_second_iteration_uses_its_own_momentum():
     assert np.abs(res.final_locations - x1).max() <= 1e-9 * max(1.0, np.abs(x1).max())
 
 
-def test_fp32_chain_consistent_with_oracle():
-    n, p, tau = 400, 2, 1.0
+@pytest.mark.parametrize("p", [2, 6])
+def test_fp32_chain_consistent_with_oracle(p):
+    # P = 6: the column-pack pair math with the fused kick/drift
+    n, tau = 400, 1.0
     delta, x0 = _problem(n, p, 7, clusters=5)
     e = _engine(delta.astype(np.float32), p, tau, F.FLOAT)
     res = hmc(e, x0, iterations=30, leapfrog_steps=10, step_size=0.002, seed=3)
