@@ -451,7 +451,7 @@ using PairMathF32For =
 
 // ------------------------------------------------------------ FP64 pair math
 
-// One unordered pair {i, j} in FP64 (CUDA double rsqrt, erfc, exp; one
+// One unordered pair {i, j} in FP64 (CUDA double rsqrt, erfcx, exp; one
 // division), both directions: dA = delta_ij, dB = delta_ji.
 // With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
 // -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
@@ -479,8 +479,8 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
     double t = 0.0;
     if (TRUNC) {
         const double z = d * sqrt_tau;
-        const double cdf = 0.5 * erfc(-z * 0.70710678118654752440);
-        const double pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
+        double cdf, pdf;
+        normal_cdf_pdf_f64(z, cdf, pdf);
         if (MASKED) {
             if (vA) prodm *= cdf;
             if (vB) prodm *= cdf;

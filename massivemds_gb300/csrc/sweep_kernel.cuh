@@ -34,7 +34,7 @@
 // giving 1/Phi); logPhi summed as log2 of running products of 1/Phi (one lg2
 // per 64 pairs); r^2 sums compensated with TwoSum; per-tile partials promoted to
 // FP64 for every reduction above the warp. FP64 mode: pair arithmetic in FP64
-// with CUDA's double sqrt/erfc/exp/log.
+// with CUDA's double sqrt/erfcx/exp/log (Phi through erfcx, normal_cdf_pdf_f64).
 #pragma once
 
 #include <cstdint>
@@ -215,7 +215,16 @@ __device__ __forceinline__ void pair2_f32(const f2 (&xi)[P], const f2 (&xj)[P], 
     for (int q = 0; q < P; ++q) g[q] = ffma2(c, dx[q], g[q]);
 }
 
-// One ordered pair in FP64 (CUDA double sqrt/erfc/exp). log Phi is not taken
+// Normal CDF and density at z >= 0 in FP64 with one exponential:
+// Phi(z) = 1 - Q(z), Q(z) = phi(z) sqrt(pi/2) erfcx(z / sqrt 2), from
+// erfc(x) = exp(-x^2) erfcx(x); the exponential of the density serves both
+// (CUDA's erfc would evaluate its own). |Phi - (1 - erfc(z / sqrt 2) / 2)| <= 5e-16.
+__device__ __forceinline__ void normal_cdf_pdf_f64(double z, double& cdf, double& pdf) {
+    pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
+    cdf = 1.0 - pdf * 1.2533141373155002512 * erfcx(z * 0.70710678118654752440);
+}
+
+// One ordered pair in FP64 (CUDA double sqrt/erfcx/exp). log Phi is not taken
 // per pair: Phi multiplies into lprod (Phi >= 1/2 for d >= 0) and the caller
 // folds log(lprod) into the row's sum every kLogFoldF64Stages stages.
 template <int P, bool TRUNC, bool MASKED>
@@ -235,9 +244,9 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
     double cc;
     if (TRUNC) {
         const double z = d * sqrt_tau;
-        const double cdf = 0.5 * erfc(-z * 0.70710678118654752440);
+        double cdf, pdf;
+        normal_cdf_pdf_f64(z, cdf, pdf);
         lprod *= cdf;
-        const double pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
         // (res - pdf / (cdf sqrt_tau)) / d with one division
         const double den = cdf * sqrt_tau;
         cc = fma(res, den, -pdf) / (den * d);
