@@ -158,6 +158,13 @@ int mdsx_get_sweep_schedule(mdsx_engine* engine, int* out);
  * designed (the context stays usable), MDSX_ECUDA otherwise. */
 int mdsx_selftest_bounded_wait(double limit_seconds, int device, int* device_code);
 
+/* Self-test of the FP64 pair-math helpers (no counterpart in the reference):
+ * for each of the n host values x[i] writes out[4i .. 4i+3] = the sweep's
+ * Newton-refined 1/x and 1/sqrt(x), and its normal CDF and density at z = x
+ * (the FP64 sweeps' Phi and phi), computed on `device` (< 0: current).
+ * Returns MDSX_OK, MDSX_EINVAL (n = 0 or > 2^24), MDSX_ENOMEM or MDSX_ECUDA. */
+int mdsx_selftest_math_f64(const double* x, size_t n, double* out, int device);
+
 /* ---- Learned gradient surrogate (no counterpart in the reference) ----
  * g_i ~= s * sum_k alpha_ik (x_i - x_{l_k}) over K landmark locations (a
  * seeded random subset), alpha_i = MLP(features_i) with rotation-invariant

@@ -50,6 +50,7 @@ SIGNATURES = {
     "mdsx_set_sweep_schedule": (_i, [_vp, _i]),
     "mdsx_get_sweep_schedule": (_i, [_vp, _ip]),
     "mdsx_selftest_bounded_wait": (_i, [ctypes.c_double, _i, _ip]),
+    "mdsx_selftest_math_f64": (_i, [_dp, _sz, _dp, _i]),
     "mdsx_hmc_run": (_i, [_vp, _vp, _dp, _dp, _dp, _vp]),
     "mdsx_sweep_f32_noalloc": (_i, [_vp, ctypes.c_longlong, _vp, _i, _i, ctypes.c_double, _i, _vp, _vp, _vp]),
     "mdsx_version": (ctypes.c_char_p, []),

@@ -451,8 +451,8 @@ using PairMathF32For =
 
 // ------------------------------------------------------------ FP64 pair math
 
-// One unordered pair {i, j} in FP64 (CUDA double rsqrt, erfcx, exp; one
-// division), both directions: dA = delta_ij, dB = delta_ji.
+// One unordered pair {i, j} in FP64 (rsqrt_f64, rcp_f64, CUDA's erfcx and exp; one
+// reciprocal), both directions: dA = delta_ij, dB = delta_ji.
 // With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
 // -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
 // into cacc (signs as in the FP32 policy). Fast path: Phi multiplies into prod
@@ -469,10 +469,10 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
 #pragma unroll
     for (int q = 1; q < P; ++q) d2 = fma(dx[q], dx[q], d2);
     if (MASKED && !(vA || vB)) return;
-    const double rs = rsqrt(d2);
+    const double rs = rsqrt_f64(d2);
     // coincident points (d2 = 0, i != j): d = 0 as the reference's sqrt gives, so the
-    // likelihood term is finite; rs = inf makes their gradient terms NaN, as the reference's
-    const double d = d2 > 0.0 ? d2 * rs : 0.0;
+    // likelihood term is finite; rs = NaN makes their gradient terms NaN, as the reference's
+    const double d = d2 >= kMinNormalF64 ? d2 * rs : 0.0;
     const double resA = dA - d, resB = dB - d;
     if (!MASKED || vA) r2 = fma(resA, resA, r2);
     if (!MASKED || vB) r2 = fma(resB, resB, r2);
@@ -487,7 +487,7 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
         } else {
             prod *= cdf;
         }
-        t = pdf * rs / (cdf * sqrt_tau);
+        t = pdf * rs * rcp_f64(cdf * sqrt_tau);
     }
     if (!MASKED || vA) {
         const double nc = fma(-resA, rs, t);

@@ -140,6 +140,28 @@ __device__ __forceinline__ float lg2_approx(float x) {
     return y;
 }
 
+// FP64 reciprocal and reciprocal square root for finite x >= the smallest
+// normal double: the hardware approximation (rcp.approx.ftz.f64,
+// rsqrt.approx.ftz.f64) refined by one third-order Newton step, which cubes the
+// seed's relative error e:
+//   1/x       = y / (1 - e),       e = 1 - x y,    y += y (e + e^2)
+//   1/sqrt(x) = y (1 - e)^(-1/2),  e = 1 - x y^2,  y += y e (1/2 + 3e/8)
+// x = 0 (and x below the normal range, flushed to 0) gives NaN.
+__device__ __forceinline__ double rcp_f64(double x) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
+}
+__device__ __forceinline__ double rsqrt_f64(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x * y, y, 1.0);
+    return fma(y * e, fma(0.375, e, 0.5), y);
+}
+// Smallest normal double: squared distances below it count as coincident points.
+constexpr double kMinNormalF64 = 2.2250738585072014e-308;
+
 // Error-free transformation a + b = s + e (Knuth's TwoSum).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = a + b;

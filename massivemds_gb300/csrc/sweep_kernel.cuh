@@ -34,7 +34,8 @@
 // giving 1/Phi); logPhi summed as log2 of running products of 1/Phi (one lg2
 // per 64 pairs); r^2 sums compensated with TwoSum; per-tile partials promoted to
 // FP64 for every reduction above the warp. FP64 mode: pair arithmetic in FP64
-// with CUDA's double sqrt/erfcx/exp/log (Phi through erfcx, normal_cdf_pdf_f64).
+// with CUDA's double erfcx/exp/log (Phi through erfcx, normal_cdf_pdf_f64) and
+// Newton-refined reciprocals (rcp_f64, rsqrt_f64).
 #pragma once
 
 #include <cstdint>
@@ -224,7 +225,7 @@ __device__ __forceinline__ void normal_cdf_pdf_f64(double z, double& cdf, double
     cdf = 1.0 - pdf * 1.2533141373155002512 * erfcx(z * 0.70710678118654752440);
 }
 
-// One ordered pair in FP64 (CUDA double sqrt/erfcx/exp). log Phi is not taken
+// One ordered pair in FP64 (rsqrt_f64, rcp_f64, CUDA's erfcx and exp). log Phi is not taken
 // per pair: Phi multiplies into lprod (Phi >= 1/2 for d >= 0) and the caller
 // folds log(lprod) into the row's sum every kLogFoldF64Stages stages.
 template <int P, bool TRUNC, bool MASKED>
@@ -238,7 +239,10 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
 #pragma unroll
     for (int q = 1; q < P; ++q) d2 = fma(dx[q], dx[q], d2);
     if (MASKED && !valid) return;
-    const double d = sqrt(d2);
+    // coincident points (d2 = 0): d = 0 as the reference's sqrt gives; rs is NaN,
+    // so their gradient terms are NaN where the reference's divide by d = 0
+    const double rs = rsqrt_f64(d2);
+    const double d = d2 >= kMinNormalF64 ? d2 * rs : 0.0;
     double res = delta - d;
     r2 = fma(res, res, r2);
     double cc;
@@ -247,11 +251,11 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
         double cdf, pdf;
         normal_cdf_pdf_f64(z, cdf, pdf);
         lprod *= cdf;
-        // (res - pdf / (cdf sqrt_tau)) / d with one division
+        // (res - pdf / (cdf sqrt_tau)) / d
         const double den = cdf * sqrt_tau;
-        cc = fma(res, den, -pdf) / (den * d);
+        cc = fma(res, den, -pdf) * rs * rcp_f64(den);
     } else {
-        cc = res / d;
+        cc = res * rs;
     }
 #pragma unroll
     for (int q = 0; q < P; ++q) g[q] = fma(cc, dx[q], g[q]);

@@ -428,6 +428,40 @@ def test_bounded_wait_gives_up_and_context_stays_usable():
     e.close()
 
 
+def test_fp64_math_helpers():
+    """The FP64 sweeps' Newton-refined reciprocal and reciprocal square root
+    within 2 ulp of the correctly rounded values over the normal range, and their
+    normal CDF / density (Phi through erfcx with the density's exponential)
+    within 1e-15 absolute / the exponential's argument rounding of the exact
+    values; 0 gives NaN reciprocals (coincident points)."""
+    import ctypes
+    from scipy.special import ndtr
+    from massivemds_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(70)
+    x = np.concatenate([10.0 ** rng.uniform(-307, 307, 200000), rng.uniform(0.0, 40.0, 100000),
+                        np.linspace(0.0, 9.0, 9001), [0.0, 1.0, 2.0, 0.5, 4.0, np.nextafter(1.0, 2.0),
+                                                      np.nextafter(1.0, 0.0), 2.2250738585072014e-308, 38.6, 50.0,
+                                                      1e3]])
+    out = np.empty((x.size, 4))
+    dp = ctypes.POINTER(ctypes.c_double)
+    assert lib.mdsx_selftest_math_f64(x.ctypes.data_as(dp), x.size, out.ctypes.data_as(dp), -1) == 0
+    pos = x >= 2.2250738585072014e-308
+    xl = x[pos].astype(np.longdouble)
+    ulp = 2.0 ** -52
+    rcp_err = np.abs((out[pos, 0] - 1 / xl) * xl)
+    rsq_err = np.abs((out[pos, 1] - 1 / np.sqrt(xl)) * np.sqrt(xl))
+    assert rcp_err.max() <= 2 * ulp and rsq_err.max() <= 2 * ulp, (rcp_err.max() / ulp, rsq_err.max() / ulp)
+    assert np.isnan(out[x == 0.0, 0]).all() and np.isnan(out[x == 0.0, 1]).all()
+    z = x[x <= 1e3]
+    assert np.abs(out[x <= 1e3, 2] - ndtr(z)).max() <= 1e-15
+    zl = z.astype(np.longdouble)
+    pdf = np.exp(-0.5 * zl * zl) / np.sqrt(2 * np.pi, dtype=np.longdouble)
+    pdf_err = np.abs(out[x <= 1e3, 3] - pdf)
+    bound = (0.5 * z * z + 4.0) * ulp * pdf + 1e-300
+    assert np.all(pdf_err <= bound), float(np.max(pdf_err / bound))
+
+
 def test_coincident_points():
     """Two distinct rows at the same location (d = 0 for a non-missing pair): the
     reference takes d = sqrt(0) = 0, so the likelihood term is finite, and
