@@ -462,6 +462,23 @@ def test_fp64_math_helpers():
     assert np.all(pdf_err <= bound), float(np.max(pdf_err / bound))
 
 
+@pytest.mark.parametrize("mode", ["f64rows", "f64pairs", "f64s32pairs", "f32pairs"])
+@pytest.mark.parametrize("tau", [1e-4, 400.0])
+def test_truncation_tails(mode, tau):
+    """z = d sqrt(tau) near 0 (Phi ~ 1/2 for every pair) and far in the tail
+    (z up to ~100: phi underflows, Phi = 1, the truncation terms vanish), with
+    missing pairs and an asymmetric delta, against the oracle at the mode's bar."""
+    n, p = 150, 2
+    delta, x = _inputs(n, p, seed=80, nans=6, asym=True)
+    tol_s, tol_g = tolerances(mode)
+    e = make_engine(n, p, True, mode, delta, x, tau)
+    s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
+    e.close()
+    d = oracle_delta(delta, mode)
+    assert rel(s, oracle.sum_of_increments(d, x, tau)) < tol_s
+    assert grad_rel(g, oracle.gradient(d, x, tau)) < tol_g
+
+
 def test_coincident_points():
     """Two distinct rows at the same location (d = 0 for a non-missing pair): the
     reference takes d = sqrt(0) = 0, so the likelihood term is finite, and
