@@ -108,6 +108,7 @@ void free_all(mdsx_engine* e) {
     cudaFree(e->d_pair_jfirst);
     cudaFree(e->d_pair_jslots);
     if (e->h_out) cudaFreeHost(e->h_out);
+    if (e->h2d_done) cudaEventDestroy(e->h2d_done);
     if (e->own_stream) cudaStreamDestroy(e->own_stream);
 }
 
@@ -422,6 +423,8 @@ int mdsx_create(int embedding_dimension, int location_count, long flags, int dev
         rc = cuda_fail(e, err, "cudaDeviceGetAttribute");
     if (!rc && (err = cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
         rc = cuda_fail(e, err, "cudaStreamCreate");
+    if (!rc && (err = cudaEventCreateWithFlags(&e->h2d_done, cudaEventDisableTiming)) != cudaSuccess)
+        rc = cuda_fail(e, err, "cudaEventCreate");
     if (!rc) {
         e->stream = e->own_stream;
         rc = plan_and_allocate(e);
@@ -458,15 +461,18 @@ int mdsx_update_locations(mdsx_engine* e, int index, const double* x, size_t len
     if (index == -1) {
         if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "updateLocations(-1): length != N*P");
         MDSX_CUDA(e, cudaMemcpyAsync(e->d_xin, x, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        MDSX_CUDA(e, cudaEventRecord(e->h2d_done, e->stream));
         MDSX_CUDA(e, mdsx::convert_locations(e->d_xin, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
     } else {
         if (index < 0 || index >= e->n) return fail(e, MDSX_EINVAL, "updateLocations: index out of range");
         if (length != (size_t)e->p) return fail(e, MDSX_EINVAL, "updateLocations(i): length != P");
         MDSX_CUDA(e, cudaMemcpyAsync(e->d_xin, x, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+        MDSX_CUDA(e, cudaEventRecord(e->h2d_done, e->stream));
         MDSX_CUDA(e, mdsx::set_one_location(e->d_xin, index, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
     }
-    // The host buffer may be reused by the caller as soon as we return.
-    MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
+    // The host buffer may be reused by the caller as soon as we return: wait for
+    // the copy only; the conversion runs on, ahead of the caller's next call.
+    MDSX_CUDA(e, cudaEventSynchronize(e->h2d_done));
     e->sum_known = false;
     e->grad_known = false;
     return MDSX_OK;

@@ -24,6 +24,7 @@ struct mdsx_engine {
     bool delta_f32 = false, x_f32 = false;
 
     cudaStream_t own_stream = nullptr;
+    cudaEvent_t h2d_done = nullptr;  // recorded after the copy of a caller's host locations
     cudaStream_t stream = nullptr;
     int sm_count = 0;
 
