@@ -131,7 +131,7 @@ class Batch:
         return sc.value, rw.value, ctas.value, grid.value
 
     def force_shape(self, p: int, rows_per_warp: int, ctas_per_sm: int = 2, schedule: int = 1) -> None:
-        """Fixes dimension p's shape (schedule 2 needs P <= 4 and rows_per_warp 4);
+        """Fixes dimension p's shape (schedule 2 needs P <= 6 and rows_per_warp 4);
         rows_per_warp 0 removes the override."""
         self._check(self._lib.mdsx_batch_force_shape(self._h, int(p), int(schedule), int(rows_per_warp),
                                                      int(ctas_per_sm)))
