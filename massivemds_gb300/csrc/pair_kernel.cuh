@@ -451,8 +451,8 @@ using PairMathF32For =
 
 // ------------------------------------------------------------ FP64 pair math
 
-// One unordered pair {i, j} in FP64 (rsqrt_f64, rcp_f64, CUDA's erfcx and exp; one
-// reciprocal), both directions: dA = delta_ij, dB = delta_ji.
+// One unordered pair {i, j} in FP64 (rsqrt_f64, rcp_f64, normal_cdf_pdf_f64 with
+// CUDA's exp), both directions: dA = delta_ij, dB = delta_ji.
 // With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
 // -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
 // into cacc (signs as in the FP32 policy). Fast path: Phi multiplies into prod
@@ -700,8 +700,16 @@ constexpr int pair_min_ctas() {
     return (P == 4 || P == 6) ? 1 : 2;
 }
 
+// FP64 pair math runs one CTA per SM at up to 255 registers: the FP64 pipe bounds
+// it, so two warps per scheduler keep the pipe busy, and at 128 registers P <= 3
+// spill 400-700 bytes (same time at N = 1000 and 20 000, one CTA slightly ahead).
+template <int P, class M>
+constexpr int pair_min_ctas_of() {
+    return std::is_same<typename M::Part, double>::value ? 1 : pair_min_ctas<P>();
+}
+
 template <int P, bool TRUNC, class M>
-__global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>())
+__global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
     pair_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
                 const __grid_constant__ CUtensorMap tmap_xi, const __grid_constant__ CUtensorMap tmap_xj,
                 const PairArgs a) {

@@ -34,14 +34,15 @@
 // giving 1/Phi); logPhi summed as log2 of running products of 1/Phi (one lg2
 // per 64 pairs); r^2 sums compensated with TwoSum; per-tile partials promoted to
 // FP64 for every reduction above the warp. FP64 mode: pair arithmetic in FP64
-// with CUDA's double erfcx/exp/log (Phi through erfcx, normal_cdf_pdf_f64) and
-// Newton-refined reciprocals (rcp_f64, rsqrt_f64).
+// with CUDA's double exp/log, Phi from our Mills-ratio fit (normal_cdf_pdf_f64)
+// and Newton-refined reciprocals (rcp_f64, rsqrt_f64).
 #pragma once
 
 #include <cstdint>
 #include <cuda.h>
 
 #include "ptx.cuh"
+#include "normal_mills_f64.h"
 
 namespace mdsx {
 
@@ -217,15 +218,17 @@ __device__ __forceinline__ void pair2_f32(const f2 (&xi)[P], const f2 (&xj)[P], 
 }
 
 // Normal CDF and density at z >= 0 in FP64 with one exponential:
-// Phi(z) = 1 - Q(z), Q(z) = phi(z) sqrt(pi/2) erfcx(z / sqrt 2), from
-// erfc(x) = exp(-x^2) erfcx(x); the exponential of the density serves both
-// (CUDA's erfc would evaluate its own). |Phi - (1 - erfc(z / sqrt 2) / 2)| <= 5e-16.
+// Phi(z) = 1 - Q(z), Q(z) = phi(z) R(z) with R the Mills ratio from our rational
+// fit (normal_mills_f64.h, evaluated at min(z, 8.5), where Q < 1e-17 beyond);
+// the exponential of the density serves both. |Phi - Phi_exact| <= 1e-15.
 __device__ __forceinline__ void normal_cdf_pdf_f64(double z, double& cdf, double& pdf) {
     pdf = 0.39894228040143267794 * exp(-0.5 * z * z);
-    cdf = 1.0 - pdf * 1.2533141373155002512 * erfcx(z * 0.70710678118654752440);
+    double num, den;
+    mills_ratio_f64(fmin(z, kMillsClamp), num, den);
+    cdf = 1.0 - pdf * num * rcp_f64(den);
 }
 
-// One ordered pair in FP64 (rsqrt_f64, rcp_f64, CUDA's erfcx and exp). log Phi is not taken
+// One ordered pair in FP64 (rsqrt_f64, rcp_f64, the Mills-ratio fit and CUDA's exp). log Phi is not taken
 // per pair: Phi multiplies into lprod (Phi >= 1/2 for d >= 0) and the caller
 // folds log(lprod) into the row's sum every kLogFoldF64Stages stages.
 template <int P, bool TRUNC, bool MASKED>

@@ -431,9 +431,10 @@ def test_bounded_wait_gives_up_and_context_stays_usable():
 def test_fp64_math_helpers():
     """The FP64 sweeps' Newton-refined reciprocal and reciprocal square root
     within 2 ulp of the correctly rounded values over the normal range, and their
-    normal CDF / density (Phi through erfcx with the density's exponential)
-    within 1e-15 absolute / the exponential's argument rounding of the exact
-    values; 0 gives NaN reciprocals (coincident points)."""
+    normal CDF / density (Phi = 1 - phi R with R the Mills-ratio fit, whose error
+    in Q is 9.4e-16 evaluated in double) within 2e-15 absolute / the
+    exponential's argument rounding of the exact values; 0 gives NaN
+    reciprocals (coincident points)."""
     import ctypes
     from scipy.special import ndtr
     from massivemds_gb300 import _lib
@@ -454,7 +455,7 @@ def test_fp64_math_helpers():
     assert rcp_err.max() <= 2 * ulp and rsq_err.max() <= 2 * ulp, (rcp_err.max() / ulp, rsq_err.max() / ulp)
     assert np.isnan(out[x == 0.0, 0]).all() and np.isnan(out[x == 0.0, 1]).all()
     z = x[x <= 1e3]
-    assert np.abs(out[x <= 1e3, 2] - ndtr(z)).max() <= 1e-15
+    assert np.abs(out[x <= 1e3, 2] - ndtr(z)).max() <= 2e-15
     zl = z.astype(np.longdouble)
     pdf = np.exp(-0.5 * zl * zl) / np.sqrt(2 * np.pi, dtype=np.longdouble)
     pdf_err = np.abs(out[x <= 1e3, 3] - pdf)
