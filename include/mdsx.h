@@ -140,9 +140,9 @@ int mdsx_last_launch_count(mdsx_engine* engine, int* out);
  *   MDSX_SWEEP_ROWS  - one pass per ordered pair, row blocks x 128-column stages;
  *   MDSX_SWEEP_PAIRS - each unordered pair {i, j} once: distance and Phi shared
  *                      by (i, j) and (j, i), each direction with its own delta;
- *                      a sweep kernel plus a finish kernel. P <= 6 with FP32
- *                      pair math, P <= 4 with FP64 pair math (FP64 results
- *                      within 1e-10 of the row-block schedule's).
+ *                      a sweep kernel plus a finish kernel, for P <= 6 in
+ *                      every precision mode (FP64 results within 1e-10 of
+ *                      the row-block schedule's).
  * New engines use MDSX_SWEEP_PAIRS where it is built and truncation is on (the
  * pair math dominates there), else MDSX_SWEEP_ROWS.
  * Setting MDSX_SWEEP_PAIRS where it is not built returns MDSX_EUNSUPPORTED. */

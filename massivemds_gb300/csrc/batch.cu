@@ -11,7 +11,7 @@
 // instances (batch_kernel.cuh), a queue of whole row blocks taken
 // dynamically, largest instance first (batch_queue.cuh), and stream-K over the
 // unordered-pair units of all instances with a finish kernel (batch_pairs.cuh,
-// P <= 4). Results of all instances come back in one
+// P <= 6). Results of all instances come back in one
 // device-to-host copy. Instance calls keep the reference's names and lazy
 // semantics: a getter evaluates the batch when any instance changed.
 //
@@ -410,7 +410,7 @@ int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
 }
 
 // Shape of a group: the override, else the tuning cache, else the default: with
-// truncation and P <= 4 the unordered-pair schedule (the single-instance
+// truncation and P <= 6 the unordered-pair schedule (the single-instance
 // engine's choice), otherwise the row-block queue with the single-instance rows
 // per warp; full occupancy.
 Shape group_shape(const mdsx_batch* b, int p, double mean_n, const std::map<std::pair<int, int>, Shape>* force) {
@@ -1060,7 +1060,7 @@ extern "C" {
 
 // Test and tuning hook: fixes the shape of the group of embedding dimension p:
 // schedule (0 stream-K, 1 row-block queue, 2 unordered pairs with rows per warp 4,
-// P <= 4), rows per warp, CTAs per SM; rows_per_warp 0 removes the override.
+// P <= 6), rows per warp, CTAs per SM; rows_per_warp 0 removes the override.
 int mdsx_batch_force_shape(mdsx_batch* b, int p, int schedule, int rows_per_warp, int ctas_per_sm) {
     if (!b) return MDSX_EINVAL;
     const std::pair<int, int> key{p, b->trunc ? 1 : 0};

@@ -675,7 +675,7 @@ int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
     if (schedule != MDSX_SWEEP_ROWS && schedule != MDSX_SWEEP_PAIRS)
         return fail(e, MDSX_EINVAL, "unknown sweep schedule");
     if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
-        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for P <= 6 (FP32) and P <= 4 (FP64 modes) only");
+        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for P <= 6 only");
     if (schedule != e->schedule) {
         e->schedule = schedule;
         e->sum_known = e->grad_known = false;

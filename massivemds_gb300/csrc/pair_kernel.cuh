@@ -58,7 +58,7 @@ constexpr int kPairRows = 32;   // rows per chunk I: 8 warps x 4
 constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
 constexpr int kPairMaxP = 6;     // FP32 pair math: P <= 4 row packs (PairMathF32), 5..6 column packs
-constexpr int kPairMaxP64 = 4;   // FP64 pair math
+constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_ctas_of)
 
 // XB: bytes per location element (4: FP32 math, 8: FP64 math); SB: bytes per
 // delta element. FP64 math is bound by the FP64 pipe, so two stages hide the

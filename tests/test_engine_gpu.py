@@ -7,7 +7,7 @@ Tolerances (from the engine's stated targets):
   FP32 mode (FP32 pairs, compensated FP32 partials, FP64 reductions): within
     1e-5 relative of the FP64 oracle on the same (FP32-rounded) delta, with
     either sweep schedule: "f32" is the engine's default (unordered pairs for
-    P <= 4 with truncation, else row blocks), "f32rows" and "f32pairs" force one;
+    P <= 6 with truncation, else row blocks), "f32rows" and "f32pairs" force one;
     the same for FP64 over FP32-stored delta ("f64s32", "f64s32rows", "f64s32pairs")
     and over FP64-stored delta ("f64", "f64rows", "f64pairs").
 """
@@ -67,7 +67,7 @@ def test_fp64_matches_reference_golden(golden, mode):
         if use_float:
             continue
         n, p = int(n), int(p)
-        if mode == "f64pairs" and p > 4:
+        if mode == "f64pairs" and p > 6:
             continue
         e = make_engine(n, p, bool(trunc), mode, data[f"{name}.delta"], data[f"{name}.x"], tau)
         s = e.getSumOfIncrements()
@@ -152,8 +152,8 @@ def test_sizes_and_edges(mode, n):
 @pytest.mark.parametrize("mode", ["f64rows", "f64pairs", "f32rows", "f32pairs", "f64s32pairs"])
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6, 7, 8, 9, 10])
 def test_dimensions(mode, p):
-    if mode.endswith("pairs") and p > (6 if mode == "f32pairs" else 4):
-        pytest.skip("the unordered-pair schedule is built for P <= 6 (FP32) and P <= 4 (FP64)")
+    if mode.endswith("pairs") and p > 6:
+        pytest.skip("the unordered-pair schedule is built for P <= 6")
     n, tau = 300, 0.8
     delta, x = _inputs(n, p, seed=100 + p, nans=2, asym=True)
     tol_s, tol_g = tolerances(mode)
@@ -299,7 +299,7 @@ def test_error_statuses():
 
 def test_sweep_schedules():
     """Truncated engines default to the unordered-pair schedule (sweep + finish
-    kernel) where it is built (FP32: P <= 6; FP64: P <= 4), untruncated ones to
+    kernel) where it is built (P <= 6), untruncated ones to
     the row-block schedule; beyond that range the engine runs the row-block
     schedule and refuses the pair schedule; switching invalidates the cached
     results."""
@@ -311,8 +311,9 @@ def test_sweep_schedules():
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
     e.close()
     for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (6, "f32", F.SWEEP_PAIRS),
-                             (7, "f32", F.SWEEP_ROWS), (2, "f64", F.SWEEP_PAIRS), (5, "f64", F.SWEEP_ROWS),
-                             (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_ROWS)):
+                             (7, "f32", F.SWEEP_ROWS), (2, "f64", F.SWEEP_PAIRS), (6, "f64", F.SWEEP_PAIRS),
+                             (7, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_PAIRS),
+                             (8, "f64s32", F.SWEEP_ROWS)):
         delta, x = _inputs(n, p, seed=30 + p)
         e = make_engine(n, p, True, mode, delta, x, tau)
         assert e.sweep_schedule() == default, (p, mode)

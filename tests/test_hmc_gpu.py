@@ -43,10 +43,10 @@ def test_one_trajectory_matches_restatement(use_graph):
     assert abs(res.column("log_likelihood")[0] - oracle.log_likelihood(s, n, tau)) < 1e-8 * abs(s)
 
 
-@pytest.mark.parametrize("p", [1, 3, 4])
+@pytest.mark.parametrize("p", [1, 3, 4, 6])
 def test_second_iteration_uses_its_own_momentum(p):
-    # the truncated FP64 engine runs the unordered-pair sweep for P <= 4, whose
-    # finish kernel applies the kick/drift: P = 4 is its widest instance
+    # the truncated FP64 engine runs the unordered-pair sweep for P <= 6, whose
+    # finish kernel applies the kick/drift: P = 6 is its widest instance
     n, tau, eps, steps, seed = 50, 0.9, 0.003, 8, 5
     delta, x0 = _problem(n, p, 6)
     e = _engine(delta, p, tau, 0)
