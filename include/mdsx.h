@@ -143,8 +143,9 @@ int mdsx_last_launch_count(mdsx_engine* engine, int* out);
  *                      a sweep kernel plus a finish kernel, for P <= 6 in
  *                      every precision mode (FP64 results within 1e-10 of
  *                      the row-block schedule's).
- * New engines use MDSX_SWEEP_PAIRS where it is built and truncation is on (the
- * pair math dominates there), else MDSX_SWEEP_ROWS.
+ * New engines use MDSX_SWEEP_PAIRS where it is built, in the FP64 modes and in
+ * FP32 with truncation (the pair math dominates there), else MDSX_SWEEP_ROWS
+ * (untruncated FP32, at the memory bound with one kernel).
  * Setting MDSX_SWEEP_PAIRS where it is not built returns MDSX_EUNSUPPORTED. */
 #define MDSX_SWEEP_ROWS 0
 #define MDSX_SWEEP_PAIRS 1

@@ -219,9 +219,11 @@ int plan_and_allocate(mdsx_engine* e) {
         rc = plan_pairs(e);
         if (rc) return rc;
         // Measured on GB300: with truncation the pair math dominates and sharing it between
-        // (i, j) and (j, i) wins by 17-29 % (N = 5 000 .. 50 000, P = 1 .. 4); without it the
-        // row-block sweep is already at the memory bound and its single kernel is faster.
-        if (e->trunc) e->schedule = MDSX_SWEEP_PAIRS;
+        // (i, j) and (j, i) wins by 17-29 % in FP32 (N = 5 000 .. 50 000, P = 1 .. 4); without it
+        // the FP32 row-block sweep is already at the memory bound and its single kernel is
+        // faster. FP64 is bound by the FP64 pipe either way: pairs win by 1.4x untruncated and
+        // 1.8x truncated (N = 20 000, P = 2).
+        if (e->trunc || e->mode != Mode::kF32) e->schedule = MDSX_SWEEP_PAIRS;
     }
     MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
     return MDSX_OK;

@@ -298,11 +298,11 @@ def test_error_statuses():
 
 
 def test_sweep_schedules():
-    """Truncated engines default to the unordered-pair schedule (sweep + finish
-    kernel) where it is built (P <= 6), untruncated ones to
-    the row-block schedule; beyond that range the engine runs the row-block
-    schedule and refuses the pair schedule; switching invalidates the cached
-    results."""
+    """Truncated engines and FP64 engines default to the unordered-pair
+    schedule (sweep + finish kernel) where it is built (P <= 6), untruncated
+    FP32 ones to the row-block schedule; beyond that range the engine runs the
+    row-block schedule and refuses the pair schedule; switching invalidates the
+    cached results."""
     n, tau = 300, 1.3
     delta, x = _inputs(n, 2, seed=29)
     e = make_engine(n, 2, False, "f32", delta, x, tau)
@@ -310,6 +310,12 @@ def test_sweep_schedules():
     e.set_sweep_schedule(F.SWEEP_PAIRS)
     assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(delta.astype(np.float32), x, tau, False)) < TOL_F32
     e.close()
+    for mode in ("f64", "f64s32"):
+        e = make_engine(n, 2, False, mode, delta, x, tau)
+        assert e.sweep_schedule() == F.SWEEP_PAIRS, mode
+        assert rel(e.getSumOfIncrements(), oracle.sum_of_increments(oracle_delta(delta, mode), x, tau, False)) \
+            < TOL_F64_SUM
+        e.close()
     for p, mode, default in ((2, "f32", F.SWEEP_PAIRS), (4, "f32", F.SWEEP_PAIRS), (6, "f32", F.SWEEP_PAIRS),
                              (7, "f32", F.SWEEP_ROWS), (2, "f64", F.SWEEP_PAIRS), (6, "f64", F.SWEEP_PAIRS),
                              (7, "f64", F.SWEEP_ROWS), (2, "f64s32", F.SWEEP_PAIRS), (5, "f64s32", F.SWEEP_PAIRS),
