@@ -51,7 +51,7 @@ struct mdsx_engine {
     CUtensorMap tmap_delta{};
     CUtensorMap tmap_x[2]{};
 
-    // Unordered-pair schedule (FP32, P <= 4): plan, scratch, tensor maps per location buffer.
+    // Unordered-pair schedule (P <= 6, every precision mode): plan, scratch, tensor maps per location buffer.
     int schedule = MDSX_SWEEP_ROWS;
     bool pairs_built = false;
     int pair_nb = 0, pair_nc = 0, pair_grid = 0, pair_max_slots = 0;
