@@ -340,10 +340,13 @@ int mdsx_batch_force_shape(mdsx_batch* batch, int p, int schedule, int rows_per_
  * (a cudaStream_t; NULL = the legacy default stream).
  *
  * All scratch lives in one static device array of MDSX_NOALLOC_SCRATCH_BYTES,
- * held on every GPU that loads the library until the process exits. The first
- * call on a device resolves that array's address (cudaGetSymbolAddress), so
- * make it before any stream capture. Calls share the array: calls that overlap
- * on the GPU race and must be serialised. Problems whose scratch does not fit
+ * held until the process exits on each device where the entry point has been
+ * called (on every device the process uses under CUDA_MODULE_LOADING=EAGER).
+ * Each call resolves that array's address in the current context
+ * (cudaGetSymbolAddress) and returns after the results are in the caller's
+ * buffers. Delta is read once when it holds no NaN; with NaN pairs the call
+ * scans delta for them and sweeps a second time. Calls share the array: calls
+ * that overlap on the GPU race and must be serialised. Problems whose scratch does not fit
  * (N above MDSX_NOALLOC_MAX_LOCATIONS, or a plan too large) return MDSX_EINVAL;
  * mdsx_last_error(NULL) then gives the message. No cudaMalloc, cudaFree or
  * allocating library routine is called. */

@@ -10,16 +10,26 @@
 // intermediate lives in g_noalloc_scratch below.
 //
 // Rules of use:
-//  - Every GPU that loads libmdsx.so holds kNoAllocScratchBytes of device
-//    memory for this array until the process exits.
-//  - The first call on a device resolves the array's device address with
-//    cudaGetSymbolAddress (once per device, with that device current). Make
-//    that first call before any stream capture.
+//  - The array takes kNoAllocScratchBytes on each device where this file's
+//    module is loaded: under CUDA's default lazy module loading, the devices
+//    where the entry point has been called; with CUDA_MODULE_LOADING=EAGER,
+//    every device the process uses. It is held until the process exits.
+//  - Every call resolves the array's device address with
+//    cudaGetSymbolAddress in the caller's current device and context, so a
+//    context created after cudaDeviceReset, or a non-primary context made
+//    current by the caller, gets its own module's copy.
+//  - The call is synchronous: it returns after the results are in the
+//    caller's buffers and the kernel's status word has been read back.
 //  - All calls share the one array and it keeps the previous call's contents;
 //    each call clears the counters and the error word it needs at zero. Calls
 //    whose work overlaps on the GPU (other streams, other host threads) race
 //    on the scratch: serialise them.
 //  - Sizes whose scratch does not fit are rejected with MDSX_EINVAL.
+//
+// Delta is read once per call when it holds no NaN: the sweep first runs with
+// only the padding rows marked (no scan of delta for missing pairs); a NaN
+// pair on the kernel's unmasked path then makes the sum NaN, and only in that
+// case are the NaN rows marked by a scan and the sweep run again.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -27,7 +37,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "../../include/mdsx.h"
@@ -39,9 +48,6 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = MDSX_NOALLOC_SCRATCH_BYTES;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
 int noalloc_fail(int code, const std::string& msg) {
     mdsx::set_global_error(msg);  // read back with mdsx_last_error(NULL)
     return code;
@@ -57,16 +63,12 @@ int noalloc_cuda_fail(cudaError_t err, const char* what) {
         if (_err != cudaSuccess) return noalloc_cuda_fail(_err, #call); \
     } while (0)
 
-// Device address of g_noalloc_scratch on the current device (resolved once).
-int scratch_address(int device, void** out) {
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_ptr[device]) {
-        void* ptr = nullptr;
-        cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (err != cudaSuccess) return noalloc_cuda_fail(err, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_scratch_ptr[device] = ptr;
-    }
-    *out = g_scratch_ptr[device];
+// Device address of g_noalloc_scratch in the current context.
+int scratch_address(void** out) {
+    void* ptr = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (err != cudaSuccess) return noalloc_cuda_fail(err, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *out = ptr;
     return MDSX_OK;
 }
 
@@ -122,9 +124,8 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
 
     int device = 0;
     NOALLOC_CUDA(cudaGetDevice(&device));
-    if (device >= kMaxDevices) return noalloc_fail(MDSX_EINVAL, "device index above the supported count");
     void* base = nullptr;
-    int rc = scratch_address(device, &base);
+    int rc = scratch_address(&base);
     if (rc) return rc;
 
     // Same tile plan as the engine's FP32 mode.
@@ -165,11 +166,9 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
         return noalloc_fail(MDSX_EINVAL, "problem needs " + std::to_string(off) + " bytes of scratch; the allocation-free "
                             "sweep has " + std::to_string(kNoAllocScratchBytes));
 
-    // Counters, sums and the error word must start at zero.
-    NOALLOC_CUDA(cudaMemsetAsync(out, 0, 4 * sizeof(double), stream));
-    NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
     NOALLOC_CUDA(mdsx::convert_locations(d_locations, n, p, x, x_ld, true, stream));
-    NOALLOC_CUDA(mdsx::mark_nan_rows(d_delta, true, n, delta_ld, row_nan, rows_padded, stream));
+    // First pass: only the padding rows (>= N) take the masked path.
+    NOALLOC_CUDA(mdsx::mark_padding_rows(n, row_nan, rows_padded, stream));
 
     CUtensorMap tmap_delta{}, tmap_x{};
     rc = tmap_f32(&tmap_delta, d_delta, n, n, delta_ld, mdsx::kStepCols, rb);
@@ -208,14 +207,24 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
     a.sums_out = out;
     a.truncation = truncation ? 1 : 0;
     a.err = reinterpret_cast<int*>(out + 3);
-    NOALLOC_CUDA(mdsx::sweep_launch(mdsx::Mode::kF32, p, truncation != 0, grid, tmap_delta, tmap_x, a, stream));
+    // Counters, sums and the error word must start at zero on each pass.
+    double host_out[4];
+    for (int pass = 0; pass < 2; ++pass) {
+        NOALLOC_CUDA(cudaMemsetAsync(out, 0, 4 * sizeof(double), stream));
+        NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
+        NOALLOC_CUDA(mdsx::sweep_launch(mdsx::Mode::kF32, p, truncation != 0, grid, tmap_delta, tmap_x, a, stream));
+        NOALLOC_CUDA(cudaMemcpyAsync(host_out, out, sizeof(host_out), cudaMemcpyDeviceToHost, stream));
+        NOALLOC_CUDA(cudaStreamSynchronize(stream));
+        int dev_err = 0;
+        std::memcpy(&dev_err, &host_out[3], sizeof(int));
+        if (dev_err != 0) return noalloc_fail(MDSX_ETIMEOUT, "a bounded device wait in the sweep kernel timed out");
+        // A finite sum: no NaN pair reached the unmasked path. Otherwise mark
+        // the rows holding a NaN and sweep again (NaN locations stay NaN).
+        if (!std::isnan(host_out[2]) || pass == 1) break;
+        NOALLOC_CUDA(mdsx::mark_nan_rows(d_delta, true, n, delta_ld, row_nan, rows_padded, stream));
+    }
     NOALLOC_CUDA(cudaMemcpyAsync(d_sum_of_increments, out + 2, sizeof(double), cudaMemcpyDeviceToDevice, stream));
-
-    // Synchronous like the rest of the ABI: report a device-side timeout.
-    int dev_err = 0;
-    NOALLOC_CUDA(cudaMemcpyAsync(&dev_err, out + 3, sizeof(int), cudaMemcpyDeviceToHost, stream));
     NOALLOC_CUDA(cudaStreamSynchronize(stream));
-    if (dev_err != 0) return noalloc_fail(MDSX_ETIMEOUT, "a bounded device wait in the sweep kernel timed out");
     return MDSX_OK;
 }
 

@@ -69,6 +69,11 @@ __global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int n, long lo
     }
 }
 
+__global__ void mark_padding_rows_kernel(int n, int* __restrict__ row_nan, int rows_padded) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows_padded; i += gridDim.x * blockDim.x)
+        row_nan[i] = i >= n ? 1 : 0;
+}
+
 template <typename T>
 __global__ void write_flag_row_kernel(const int* __restrict__ row_nan, int n, int rows_padded,
                                       T* __restrict__ flags, int x_ld) {
@@ -125,6 +130,11 @@ cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, i
     else
         mark_nan_rows_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(delta), n, ld, row_nan,
                                                           rows_padded);
+    return cudaGetLastError();
+}
+
+cudaError_t mark_padding_rows(int n, int* row_nan, int rows_padded, cudaStream_t s) {
+    mark_padding_rows_kernel<<<grid_for(rows_padded, 256), 256, 0, s>>>(n, row_nan, rows_padded);
     return cudaGetLastError();
 }
 

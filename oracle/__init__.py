@@ -17,6 +17,7 @@ from .oracle import (  # noqa: F401
     log_likelihood,
     port_eval_rows,
     reference_available,
+    reference_root,
     sum_of_increments,
     sweep_rows,
 )

@@ -330,3 +330,112 @@ double mdso_port_eval_rows(const void* delta, int delta_is_f32, const double* x,
     free(tid);
     return total;
 }
+
+/*
+ * The reference's FLOAT engine (NewMultiDimensionalScaling<FloatNoSimdTypeInfo, ...>,
+ * src/factory.cpp:42-62) per-evaluation work order, restated for timing as
+ * the single-precision CPU baseline: the same likelihood pass and gradient
+ * pass as mdso_port_eval_rows, with delta, locations, distances, residuals and
+ * sums in float. As in the reference, logPhi and phi take a float argument
+ * but evaluate erfc, log and exp in double (src/CDF.h:583-616: the constants
+ * M_SQRT1_2 and M_1_SQRT_2PI are double) and round the result to float.
+ * delta must be float. Returns the (unhalved) partial sum over the rows.
+ */
+typedef struct {
+    const float* delta;
+    const float* x;
+    int64_t n;
+    int p;
+    float tau;
+    int truncation;
+    int64_t t_begin, t_end, row_begin;
+    float* grad;
+    double partial;
+} port32_job;
+
+static inline float distance_f32(const float* xi, const float* xj, int p) {
+    float s = 0.0f;
+    for (int k = 0; k < p; ++k) {
+        float df = xi[k] - xj[k];
+        s += df * df;
+    }
+    return sqrtf(s);
+}
+
+static void* port32_worker(void* arg) {
+    port32_job* jb = (port32_job*)arg;
+    const int p = jb->p;
+    const float sqrt_tau = sqrtf(jb->tau), scale = 0.5f * jb->tau;
+    float total = 0.0f;
+    for (int64_t i = jb->t_begin; i < jb->t_end; ++i) {
+        const float* xi = jb->x + i * p;
+        float row = 0.0f;
+        for (int64_t j = 0; j < jb->n; ++j) {
+            const float obs = jb->delta[i * jb->n + j];
+            if (i == j || isnan(obs)) continue;
+            const float d = distance_f32(xi, jb->x + j * p, p);
+            const float r = obs - d;
+            float sq = r * r;
+            if (jb->truncation) sq = sq * scale + (float)log(0.5 * erfc(-(d * sqrt_tau) * MDSO_SQRT1_2));
+            row += sq;
+        }
+        total += row;
+        float* g = jb->grad + (i - jb->row_begin) * p;
+        for (int k = 0; k < p; ++k) g[k] = 0.0f;
+        for (int64_t j = 0; j < jb->n; ++j) {
+            const float obs = jb->delta[i * jb->n + j];
+            if (i == j || isnan(obs)) continue;
+            const float* xj = jb->x + j * p;
+            const float d = distance_f32(xi, xj, p);
+            float r = obs - d;
+            if (jb->truncation) {
+                const float z = d * sqrt_tau;
+                const float pdf = (float)(MDSO_1_SQRT_2PI * exp(-0.5 * z * z));
+                const float lphi = (float)log(0.5 * erfc(-z * MDSO_SQRT1_2));
+                r -= pdf / (expf(lphi) * sqrt_tau);
+            }
+            const float c = r * jb->tau / d;
+            for (int k = 0; k < p; ++k) g[k] += c * (xi[k] - xj[k]);
+        }
+    }
+    jb->partial = total;
+    return NULL;
+}
+
+double mdso_port_eval_rows_f32(const float* delta, const float* x, int64_t n, int p, float tau, int truncation,
+                               int64_t row_begin, int64_t row_end, float* grad, int threads) {
+    int64_t rows = row_end - row_begin;
+    if (rows <= 0) return 0.0;
+    if (threads < 1) threads = 1;
+    if (threads > rows) threads = (int)rows;
+    port32_job* jobs = (port32_job*)calloc((size_t)threads, sizeof(port32_job));
+    pthread_t* tid = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    if (!jobs || !tid) {
+        free(jobs);
+        free(tid);
+        return NAN;
+    }
+    int64_t chunk = rows / threads, extra = rows % threads, start = row_begin;
+    for (int t = 0; t < threads; ++t) {
+        port32_job* jb = &jobs[t];
+        jb->delta = delta;
+        jb->x = x;
+        jb->n = n;
+        jb->p = p;
+        jb->tau = tau;
+        jb->truncation = truncation;
+        jb->row_begin = row_begin;
+        jb->grad = grad;
+        jb->t_begin = start;
+        start += chunk + (t < extra ? 1 : 0);
+        jb->t_end = start;
+    }
+    for (int t = 1; t < threads; ++t) pthread_create(&tid[t], NULL, port32_worker, &jobs[t]);
+    port32_worker(&jobs[0]);
+    for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+    double total = 0.0;
+    for (int t = 0; t < threads; ++t) total += jobs[t].partial;
+    free(jobs);
+    free(tid);
+    return total;
+}

@@ -14,7 +14,21 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _ORACLE_SO = os.path.join(_HERE, "liboracle.so")
 _REF_SO = os.path.join(_HERE, "_ref", "libmdsref.so")
-REFERENCE_ROOT = os.environ.get("MDSX_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root() -> str | None:
+    """Root of a MassiveMDS reference checkout (its ``src/`` and ``inst/extdata``):
+    ``$MDSX_REFERENCE_ROOT`` when set, else a sibling directory named
+    ``reference`` beside this repository; None when neither holds the sources."""
+    env = os.environ.get("MDSX_REFERENCE_ROOT")
+    cands = [env] if env else [os.path.join(os.path.dirname(os.path.dirname(_HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "src", "NewMultiDimensionalScaling.hpp")):
+            return os.path.abspath(c)
+    return None
+
+
+REFERENCE_ROOT = reference_root()
 
 _dbl_p = ctypes.POINTER(ctypes.c_double)
 
@@ -23,10 +37,14 @@ def build(reference: bool | None = None) -> None:
     """Compile liboracle.so (and the reference engine when its sources exist)."""
     targets = ["oracle"]
     if reference is None:
-        reference = os.path.isdir(os.path.join(REFERENCE_ROOT, "src"))
+        reference = REFERENCE_ROOT is not None
+    args = ["make", "-s", "-C", _HERE]
     if reference:
+        if REFERENCE_ROOT is None:
+            raise RuntimeError("no reference checkout: set MDSX_REFERENCE_ROOT")
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", _HERE, f"REF={REFERENCE_ROOT}", *targets], check=True)
+        args.append(f"REF={REFERENCE_ROOT}")
+    subprocess.run([*args, *targets], check=True)
 
 
 _lib = None
@@ -137,7 +155,7 @@ def port_eval_rows(delta, x, tau, truncation, row_begin, row_end, threads=1):
 def reference_available() -> bool:
     if os.path.exists(_REF_SO):
         return True
-    if os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
+    if REFERENCE_ROOT is not None:
         try:
             build(reference=True)
         except (subprocess.CalledProcessError, OSError):

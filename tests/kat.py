@@ -13,13 +13,15 @@ from __future__ import annotations
 import os
 
 from massivemds_gb300 import formats
+from oracle import reference_root
 
-EXTDATA = os.path.join(os.environ.get("MDSX_REFERENCE_ROOT", "/root/reference"), "inst", "extdata")
+_ROOT = reference_root()
+EXTDATA = os.path.join(_ROOT, "inst", "extdata") if _ROOT else ""
 TREE_LINE = 756  # 1-based line of large.trees holding the tree of the logged state
 
 
 def available() -> bool:
-    return all(os.path.exists(os.path.join(EXTDATA, f)) for f in ("large.trees", "large.log", "h3_Deff.txt"))
+    return bool(EXTDATA) and all(os.path.exists(os.path.join(EXTDATA, f)) for f in ("large.trees", "large.log", "h3_Deff.txt"))
 
 
 def load_state():

@@ -12,7 +12,10 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(REPO, "include", "mdsx.h")
-REF_SRC = os.path.join(os.environ.get("MDSX_REFERENCE_ROOT", "/root/reference"), "src")
+from oracle import reference_root
+
+_REF_ROOT = reference_root()
+REF_SRC = os.path.join(_REF_ROOT, "src") if _REF_ROOT else None
 
 
 def declared_symbols():
@@ -107,7 +110,7 @@ def test_dropin_header_compiles_against_restated_interface():
     _compile_dropin([])
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
 def test_dropin_header_compiles_against_reference_header():
     shim = os.path.join(REPO, "oracle", "shim")
     _compile_dropin(["-DMDSX_USE_REFERENCE_HEADER", "-I", REF_SRC, "-I", shim])
