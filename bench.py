@@ -16,11 +16,21 @@ arithmetic with compensated FP32 partials and FP64 reductions.
          over the mean CUDA-event duration of its kernels (the unordered-pair
          sweep and its finish kernel, or the row-block sweep with --schedule
          rows), against the measured HBM peak.
+  parity  after the timed region: the sums of every evaluation of the last
+         timed step and the gradients of three of them, against the FP64
+         oracle on the same FP32 delta.
+  f64    the same workload in FP64 pair arithmetic over the FP32-stored delta
+         (the precision the reference's double engine computes in), timed and
+         checked against the oracle on the same states.
+  c1, c3 the reference's own benchmark case (N=1000, FP64, through the host
+         API) and the 64-instance batch, short runs with their own clocks.
   cpu_baseline  the oracle's port of the reference's per-evaluation work
          (likelihood pass + gradient pass, libm transcendentals) on all host
-         cores over a bounded sample of rows, scaled to evals/s.
+         cores over one whole evaluation, with the other CPU paths beside it
+         (one core; the reference's FLOAT engine work order; SIMD/TBB notes).
 
---impl reference times that CPU port as the reference arm.
+--impl reference times that CPU port as the reference arm: one whole
+evaluation per step.
 Multi-GPU (torchrun): every rank runs the same workload on its own GPU
 (independent replicas); value sums all ranks' evaluations over the slowest
 rank's time.
@@ -30,6 +40,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -43,10 +54,15 @@ N, P, TAU = 20000, 2, 2.0
 EVALS_PER_STEP = 200
 METRIC = "loglik+grad evals/s & HBM GB/s at N=20k; HMC minESS/s surrogate vs plain, 1 GPU"
 UNIT = "evals/s"
+PARITY_TOL = {"f32": 1e-5, "f64_sum": 1e-10, "f64_grad": 1e-9}
+
+
 def workload(n: int, precision: str = "f32", evals: int = EVALS_PER_STEP) -> str:
     math = "FP32 pairs + FP64 reductions" if precision == "f32" else "FP64 pairs (DELTA_F32 mode)"
     return (f"fused loglik+grad sweep, N={n}, P=2, tau=2, truncation, delta FP32-stored ({n * n * 4 / 1e9:.2f} GB), "
-            f"{math}, {evals} evals per step at fresh locations")
+            f"{math}, {evals} eval{'s' if evals != 1 else ''} per step at fresh locations")
+
+
 DATA = ("synthetic: delta = ||Y_i - Y_j|| + N(0, 0.05^2) noise clipped at 0, Y ~ N(0, I_10) (seed 666); "
         "x ~ N(0,1) per evaluation")
 
@@ -63,10 +79,13 @@ def parse():
                          "the same FP32-stored delta; bound by the FP64 pipe, 10 evaluations per step)")
     ap.add_argument("--schedule", default="pairs", choices=["pairs", "rows"],
                     help="sweep schedule: each unordered pair once (default) or the row-block schedule")
-    ap.add_argument("--cpu-seconds", type=float, default=4.0, help="wall time of one CPU baseline sample")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "c1"],
-                    help="sweep: the headline N=20000 FP32 sweep; c1: the reference's benchmark case "
-                         "(N=1000, FP64, 100 iterations through the host API)")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "c1", "c3"],
+                    help="sweep: the headline N=20000 line (with f64, c1 and c3 sub-objects); c1: the reference's "
+                         "benchmark case alone (N=1000, FP64, host API); c3: the 64-instance batch alone")
+    ap.add_argument("--cpu-seconds", type=float, default=3.0,
+                    help="wall time of each bounded CPU row sample (one-core and FP32 paths)")
+    ap.add_argument("--sections", default="parity,f64,c1,c3",
+                    help="comma list of the headline line's extra sections to run ('' for none)")
     return ap.parse_args()
 
 
@@ -99,6 +118,34 @@ def profiled_traffic(schedule):
     except OSError:
         pass
     return None
+
+
+def host_info():
+    """The CPU the baselines ran on."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":", 1)[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    try:
+        cc = subprocess.run(["gcc", "--version"], capture_output=True, text=True, timeout=10).stdout.splitlines()[0]
+    except (OSError, subprocess.SubprocessError, IndexError):
+        cc = None
+    return {"uname_m": platform.machine(), "nproc": os.cpu_count(), "cpu_model": model, "compiler": cc}
 
 
 class ClockSampler:
@@ -156,24 +203,104 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(inside)}
 
 
-def cpu_port_sample(delta, x_rows, tau, target_seconds):
-    """Times the oracle port over a bounded row sample; returns (evals/s, cores, sample text)."""
+def sampled(local, fn):
+    """Runs fn() with nvidia-smi sampling around it; returns (fn's result, clocks)."""
+    import torch
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.4)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    res = fn()
+    torch.cuda.synchronize()
+    t1 = time.time()
+    sampler.stop()
+    return res, sampler.summary(t0, t1)
+
+
+# ---------------------------------------------------------------- CPU paths
+
+AVX_NOTE = ("unavailable on this box ({}): the reference's SSE/AVX/AVX-512 engines need x86 and xsimd 7.1.3 "
+            "(src/AbstractMultiDimensionalScaling.hpp:13-23)")
+TBB_NOTE = ("the reference's TBB code path is timed as its work split over std::threads (no Intel TBB on this "
+            "host)")
+
+
+def cpu_port_full(delta, x, tau, threads):
+    """One whole evaluation (every row: likelihood pass + gradient pass) of the
+    oracle's FP64 port of the reference's serial per-evaluation work; seconds."""
+    import oracle
+
+    n = delta.shape[0]
+    t = time.perf_counter()
+    oracle.port_eval_rows(delta, x, tau, True, 0, n, threads=threads)
+    return time.perf_counter() - t
+
+
+def cpu_rows_rate(fn, n, target_seconds, min_rows):
+    """evals/s of fn(rows) timed on a bounded row sample, scaled by N/rows; (rate, rows, seconds)."""
+    rows = min(n, min_rows)
+    t = time.perf_counter()
+    fn(rows)
+    dt = time.perf_counter() - t
+    rows = int(min(n, max(rows, rows * target_seconds / max(dt, 1e-6))))
+    t = time.perf_counter()
+    fn(rows)
+    dt = time.perf_counter() - t
+    return (rows / n) / dt, rows, dt
+
+
+def cpu_paths(delta, x, tau, threaded_f64_value=None, target_seconds=3.0):
+    """The CPU paths beside the GPU number: the FP64 port on all threads (one
+    whole evaluation), on one thread, and the reference FLOAT engine's work
+    order on all threads (bounded row samples, scaled to evals/s)."""
+    import numpy as np
+
     import oracle
 
     n = delta.shape[0]
     cores = os.cpu_count() or 1
-    rows = max(cores, 16)
-    t = time.perf_counter()
-    oracle.port_eval_rows(delta, x_rows, tau, True, 0, rows, threads=cores)
-    dt = time.perf_counter() - t
-    rows = int(min(n, max(rows, rows * target_seconds / max(dt, 1e-6))))
-    t = time.perf_counter()
-    oracle.port_eval_rows(delta, x_rows, tau, True, 0, rows, threads=cores)
-    dt = time.perf_counter() - t
-    evals_per_s = (rows / n) / dt
-    sample = (f"rows 0..{rows - 1} of the N={n} matrix (likelihood pass + gradient pass, all {n} columns), "
-              f"{dt:.2f} s on {cores} threads, scaled by N/rows")
-    return evals_per_s, cores, sample
+    if threaded_f64_value is None:
+        threaded_f64_value = 1.0 / cpu_port_full(delta, x, tau, cores)
+    serial, s_rows, s_dt = cpu_rows_rate(lambda r: oracle.port_eval_rows(delta, x, tau, True, 0, r, threads=1),
+                                         n, target_seconds, 16)
+    d32 = delta if delta.dtype == np.float32 else delta.astype(np.float32)
+    f32, f_rows, f_dt = cpu_rows_rate(lambda r: oracle.port_eval_rows_f32(d32, x, tau, True, 0, r, threads=cores),
+                                      n, target_seconds, 4 * cores)
+    return {
+        "threaded_f64": {"value": threaded_f64_value, "unit": UNIT, "cores": cores,
+                         "sample": "one whole evaluation (all rows)"},
+        "serial_f64": {"value": serial, "unit": UNIT, "cores": 1,
+                       "sample": f"rows 0..{s_rows - 1} ({s_dt:.2f} s), scaled by N/rows"},
+        "threaded_f32": {"value": f32, "unit": UNIT, "cores": cores,
+                         "sample": f"the reference FLOAT engine's work order, rows 0..{f_rows - 1} ({f_dt:.2f} s), "
+                                   "scaled by N/rows"},
+        "avx": AVX_NOTE.format(platform.machine()) if platform.machine() not in ("x86_64", "AMD64") else
+        "unavailable: xsimd 7.1.3 is not installed",
+        "tbb": TBB_NOTE,
+        "host": host_info(),
+    }
+
+
+# ------------------------------------------------------------------ parity
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+def grad_rel(g, ref):
+    import numpy as np
+
+    g = np.asarray(g).reshape(ref.shape)
+    return float(np.abs(g - ref).max() / max(np.abs(ref).max(), 1e-300))
+
+
+def oracle_states(delta, xs, tau):
+    """(sum, gradient) of the FP64 oracle at each location set (all host threads)."""
+    import oracle
+
+    return [oracle.evaluate(delta, x, tau, True) for x in xs]
 
 
 def make_delta(n):
@@ -201,103 +328,271 @@ def job_throughput(units_per_rank: int, world: int, seconds: float) -> float:
     return units_per_rank * world / seconds
 
 
-def run_c1(args):
+# --------------------------------------------------------------------- C1
+
+def measure_c1(local, steps, warmup):
     """The reference's own benchmark case: N = 1000, P = 2, FP64, truncation,
     tau = 1, delta = distances of 1000 points iid N(0, I_10), x ~ N(0, 1); one
     iteration = updateLocations(-1, x) + getLogLikelihood() +
     getLogLikelihoodGradient() through the engine's host API (the call sequence
-    src/benchmark.cpp:250-309 times on its CPU engines). cpu_baseline: the same
+    src/benchmark.cpp:250-309 times on its CPU engines). Baseline: the same
     per-iteration work in the oracle's C port of the reference serial engine,
-    on all host threads."""
+    on all host threads and on one."""
     import numpy as np
-    import torch
 
-    rank, world, local = dist_env()
-    if rank != 0:
-        return
     import massivemds_gb300 as m
     from massivemds_gb300 import data as gen
 
     n, p, tau, iters = 1000, 2, 1.0, 100
     delta = gen.euclidean_delta(n, dim=10, seed=666)
-    xs = np.random.default_rng(667).standard_normal((args.warmup + args.steps, iters, n, p))
+    xs = np.random.default_rng(667).standard_normal((warmup + steps, iters, n, p))
     e = m.Engine(p, n, m.flags.LEFT_TRUNCATION, local)
     e.setPairwiseData(delta)
     e.setParameters([tau])
     grad = np.empty(n * p)
+    lls = np.empty((warmup + steps, iters))
 
-    def step(batch):
+    def step(s):
         for k in range(iters):
-            e.updateLocations(-1, batch[k])
-            e.getLogLikelihood()
+            e.updateLocations(-1, xs[s, k])
+            lls[s, k] = e.getLogLikelihood()
             e.getLogLikelihoodGradient(grad)
 
-    for w in range(args.warmup):
-        step(xs[w])
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    torch.cuda.synchronize()
-    t0 = time.time()
-    for s_ in range(args.steps):
-        step(xs[args.warmup + s_])
-    t1 = time.time()
-    sampler.stop()
+    for w in range(warmup):
+        step(w)
+
+    def timed():
+        t = time.perf_counter()
+        for s_ in range(steps):
+            step(warmup + s_)
+        return time.perf_counter() - t
+
+    seconds, clocks = sampled(local, timed)
     e.close()
-    sec_per_step = (t1 - t0) / args.steps
+    sec_per_step = seconds / steps
     value = iters / sec_per_step
 
-    import oracle  # cpu_baseline leg
+    import oracle  # the CPU baseline and the check of the last iteration
 
+    x_last = xs[warmup + steps - 1, iters - 1]
+    s_ref, g_ref = oracle.evaluate(delta, x_last, tau, True)
+    ll_ref = oracle.log_likelihood(s_ref, n, tau)
     cores = os.cpu_count() or 1
-    t = time.perf_counter()
-    sample_iters = 10
-    for k in range(sample_iters):
-        oracle.sum_of_increments(delta, xs[0, k], tau, True, threads=cores)
-        oracle.gradient(delta, xs[0, k], tau, True, threads=cores)
-    cpu_value = sample_iters / (time.perf_counter() - t)
-    line = {
+    base = {}
+    for label, threads in (("threaded_f64", cores), ("serial_f64", 1)):
+        t = time.perf_counter()
+        sample_iters = 10
+        for k in range(sample_iters):
+            oracle.port_eval_rows(delta, xs[0, k], tau, True, 0, n, threads=threads)
+        base[label] = {"value": sample_iters / (time.perf_counter() - t), "unit": "iterations/s", "cores": threads,
+                       "sample": f"{sample_iters} iterations of the same workload"}
+    return {
         "metric": "iterations/s (updateLocations + getLogLikelihood + getLogLikelihoodGradient)",
-        "value": value, "unit": "iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * sec_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic: delta = ||Y_i - Y_j||, Y ~ N(0, I_10) (seed 666); x ~ N(0,1) per iteration",
+        "value": value, "unit": "iterations/s", "steps": steps, "warmup": warmup,
+        "ms_per_step": 1000.0 * sec_per_step, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic: delta = ||Y_i - Y_j||, Y ~ N(0, I_10) (seed 666); x ~ N(0,1) per iteration",
         "config": {"workload": "reference benchmark case: N=1000, P=2, FP64, truncation, tau=1, 100 iterations "
                                "per step through the host API", "n": n, "p": p, "tau": tau,
                    "iterations_per_step": iters, "l2": "delta 8 MB stays in L2 (timed as a user would see it)"},
         "e2e": {"value": value, "unit": "iterations/s", "h2d_bytes_per_step": iters * n * p * 8,
                 "d2h_bytes_per_step": iters * (n * p * 8 + 8)},
-        "clocks": sampler.summary(t0, t1),
-        "cpu_baseline": {"value": cpu_value, "unit": "iterations/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample_iters} iterations of the same workload"},
+        "parity": {"loglik_rel": rel(float(lls[warmup + steps - 1, iters - 1]), ll_ref),
+                   "grad_rel": grad_rel(grad, g_ref), "iterations_checked": 1,
+                   "tolerance": [PARITY_TOL["f64_sum"], PARITY_TOL["f64_grad"]]},
+        "clocks": clocks,
+        "cpu_baseline": dict(base["threaded_f64"], kind="port", paths=base),
     }
-    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------- C3
+
+def measure_c3(local, steps, warmup, check=3):
+    """The batched workload: 64 instances, N_k ~ U{500..8000}, P cycling 2, 3,
+    6, tau_k ~ Gamma(2, 1), delta_k = distances of N_k points iid N(0, I_10),
+    FP32 with FP64 reductions, one persistent launch per dimension group in one
+    graph, shapes from the autotuner. Times the device-resident batch
+    evaluation (CUDA events) and the host API; checks `check` instances of the
+    last timed evaluation against the FP64 oracle."""
+    import numpy as np
+    import torch
+
+    from massivemds_gb300 import data as gen, flags as F
+    from massivemds_gb300.batch import Batch
+    from massivemds_gb300.batch_bench import make_instances
+
+    spec = make_instances(64, 3)
+    t0 = time.time()
+    batch = Batch(F.FLOAT | F.LEFT_TRUNCATION, local)
+    locs, deltas = [], {}
+    order = sorted(range(len(spec)), key=lambda k: spec[k][0])
+    checked = sorted({order[0], order[len(order) // 2], order[-1]}) if check else []
+    for k, (n, p, tau, s) in enumerate(spec):
+        delta = gen.pairwise_distances(gen.latent_points(n, 10, s), dtype=np.float32)
+        x = np.random.default_rng(s + 1).standard_normal((n, p))
+        batch.add_instance(p, n)
+        batch.setPairwiseData(k, delta)
+        batch.updateLocations(k, -1, x)
+        batch.setParameters(k, [tau])
+        locs.append(x)
+        if k in checked:
+            deltas[k] = delta
+        del delta
+    setup_s = time.time() - t0
+    candidates = batch.tune(repetitions=3)
+    shapes = {p: batch.group_shape(p) for p in sorted({p for _, p, _, _ in spec})}
+    dev = torch.device("cuda", local)
+    total_grad = sum(n * p for n, p, _, _ in spec)
+    d_sums = torch.empty(4 * len(spec), dtype=torch.float64, device=dev)
+    d_grads = torch.empty(total_grad, dtype=torch.float64, device=dev)
+    for _ in range(warmup):
+        batch.evaluate_device(d_sums.data_ptr(), d_grads.data_ptr())
+    torch.cuda.synchronize()
+    cur = torch.cuda.current_stream(dev)
+
+    def timed():
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(cur)
+        for _ in range(steps):
+            batch.evaluate_device(d_sums.data_ptr(), d_grads.data_ptr())
+            torch.cuda.synchronize()
+        end.record(cur)
+        torch.cuda.synchronize()
+        return start.elapsed_time(end) / 1e3 / steps
+
+    t_batch, clocks = sampled(local, timed)
+    sums = d_sums.cpu().numpy().reshape(len(spec), 4)
+    grads = d_grads.cpu().numpy()
+
+    for _ in range(2):
+        batch.evaluate()
+    t = time.perf_counter()
+    for _ in range(steps):
+        for k, x in enumerate(locs):
+            batch.updateLocations(k, -1, x)
+        batch.evaluate()
+        for k in range(len(spec)):
+            batch.getSumOfIncrements(k)
+    t_e2e = (time.perf_counter() - t) / steps
+    batch.close()
+
+    import oracle  # the check of the last timed evaluation
+
+    offs = np.cumsum([0] + [n * p for n, p, _, _ in spec])
+    worst_s = worst_g = 0.0
+    for k in checked:
+        n, p, tau, _ = spec[k]
+        s_ref, g_ref = oracle.evaluate(deltas[k], locs[k], tau, True)
+        worst_s = max(worst_s, rel(float(sums[k, 2]), s_ref))
+        worst_g = max(worst_g, grad_rel(grads[offs[k]:offs[k + 1]], g_ref))
+    bytes_per_eval = sum(4.0 * n * n for n, _, _, _ in spec)
+    hbm_peak, peak_kind = peaks()
+    gbs = bytes_per_eval / t_batch / 1e9
+    return {
+        "metric": "instance-evals/s (64-instance batch, one fused sweep of every instance)",
+        "value": len(spec) / t_batch, "unit": "instance-evals/s", "steps": steps, "warmup": warmup,
+        "ms_per_batch_eval": 1000.0 * t_batch, "higher_is_better": True, "dtype": "f32",
+        "config": {"workload": "64 instances, N ~ U{500..8000} (seed 3), P cycling 2, 3, 6, tau ~ Gamma(2, 1), "
+                               "delta = ||Y_i - Y_j|| with Y ~ N(0, I_10), FP32 delta, truncation",
+                   "sum_n2": int(sum(n * n for n, _, _, _ in spec)), "bytes_per_batch_eval": bytes_per_eval,
+                   "shapes": {str(p): {"schedule": ("stream-K", "row-block queue", "unordered pairs")[sh[0]],
+                                       "rows_per_warp": sh[1], "ctas_per_sm": sh[2], "grid": sh[3]}
+                              for p, sh in shapes.items()},
+                   "tuned_candidates": candidates, "setup_seconds": setup_s},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                     "peak_kind": peak_kind},
+        "e2e": {"value": len(spec) / t_e2e, "unit": "instance-evals/s", "ms_per_batch_eval": 1000.0 * t_e2e,
+                "h2d_bytes_per_step": sum(x.nbytes for x in locs), "d2h_bytes_per_step": 8 * (4 * len(spec) + total_grad)},
+        "parity": {"sum_rel_max": worst_s, "grad_rel_max": worst_g, "instances_checked": len(checked),
+                   "instance_sizes": [spec[k][0] for k in checked], "tolerance": PARITY_TOL["f32"]},
+        "clocks": clocks,
+    }
+
+
+# --------------------------------------------------------------- headline
+
+def measure_f64(local, delta, xs, refs, steps=10, warmup=3):
+    """FP64 pair arithmetic over the FP32-stored delta (DELTA_F32): evals/s and
+    the sweep's kernel time; the FP64 results at the checked states against
+    the oracle."""
+    import torch
+
+    import massivemds_gb300 as m
+
+    n = delta.shape[0]
+    eng = m.Engine(P, n, m.flags.DELTA_F32 | m.flags.LEFT_TRUNCATION, local)
+    eng.setPairwiseData(delta)
+    eng.setParameters([TAU])
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    dev = f"cuda:{local}"
+    pool = torch.from_numpy(xs).to(dev)
+    d_sum = torch.zeros(1, dtype=torch.float64, device=dev)
+    for k in range(warmup):
+        eng.update_locations_device(pool[k % len(xs)].data_ptr())
+        eng.evaluate_device(d_sum.data_ptr(), None)
+    torch.cuda.synchronize()
+
+    def timed():
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for k in range(steps):
+            eng.update_locations_device(pool[k % len(xs)].data_ptr())
+            ev[k][0].record(stream)
+            eng.evaluate_device(d_sum.data_ptr(), None)
+            ev[k][1].record(stream)
+        stop.record(stream)
+        torch.cuda.synchronize()
+        return start.elapsed_time(stop), statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+    (elapsed_ms, kernel_ms), clocks = sampled(local, timed)
+    eng.set_stream(None)
+    worst_s = worst_g = 0.0
+    for x, (s_ref, g_ref) in zip(xs, refs):
+        eng.updateLocations(-1, x)
+        worst_s = max(worst_s, rel(eng.getSumOfIncrements(), s_ref))
+        worst_g = max(worst_g, grad_rel(eng.getLogLikelihoodGradient(), g_ref))
+    eng.close()
+    hbm_peak, _ = peaks()
+    gbs = (float(n) * n * 4 + 2.0 * n * P * 8) / (kernel_ms / 1e3) / 1e9
+    return {"value": steps / (elapsed_ms / 1e3), "unit": UNIT, "steps": steps, "kernel_ms": kernel_ms,
+            "kernel": "pair_kernel<2,true,PairMathF64<float>> + pair_finish_kernel<2,double>",
+            "hbm_gbs": gbs, "hbm_frac": gbs / hbm_peak, "bound": "FP64 pipe",
+            "parity": {"sum_rel_max": worst_s, "grad_rel_max": worst_g, "evals_checked": len(xs),
+                       "tolerance": [PARITY_TOL["f64_sum"], PARITY_TOL["f64_grad"]]},
+            "clocks": clocks}
 
 
 def run_reference(args):
+    """The reference arm: the oracle's FP64 port of the reference serial
+    engine's per-evaluation work (a likelihood pass and a gradient pass over
+    every row) on all host threads; one step = one whole evaluation."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import numpy as np
 
     delta = make_delta(args.n)
-    x = np.random.default_rng(667).standard_normal((args.n, P))
-    vals = []
-    info = None
-    for _ in range(args.warmup + args.steps):
-        v, cores, sample = cpu_port_sample(delta, x, TAU, args.cpu_seconds)
-        vals.append(v)
-        info = (cores, sample)
-    vals = vals[args.warmup:]
-    value = statistics.mean(vals)
+    rng = np.random.default_rng(667)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_port_full(delta, rng.standard_normal((args.n, P)), TAU, cores)
+    secs = [cpu_port_full(delta, rng.standard_normal((args.n, P)), TAU, cores) for _ in range(args.steps)]
+    value = len(secs) / sum(secs)
+    paths = cpu_paths(delta, rng.standard_normal((args.n, P)), TAU, threaded_f64_value=value,
+                      target_seconds=args.cpu_seconds)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * EVALS_PER_STEP / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * statistics.mean(secs),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
-        "config": {"workload": workload(args.n).replace("FP32 pairs + FP64 reductions", "reference CPU port in FP64"),
-                   "n": args.n, "p": P, "tau": TAU, "evals_per_step": EVALS_PER_STEP},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info[0], "kind": "port", "sample": info[1]},
+        "config": {"workload": workload(args.n, evals=1).replace("FP32 pairs + FP64 reductions",
+                                                                 "reference CPU port in FP64"),
+                   "n": args.n, "p": P, "tau": TAU, "evals_per_step": 1},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} whole evaluations (every row), one per step, at fresh locations",
+                         "paths": paths},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": ("reference engine compiled from its sources is not available on this host (its sources are "
+        "note": ("the reference engine compiled from its sources is not available on this host (its sources are "
                  "not here); the oracle's port of the reference serial engine's per-evaluation work is timed"),
     }
     print(json.dumps(line), flush=True)
@@ -315,6 +610,7 @@ def run_mdsx(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     import massivemds_gb300 as m
 
+    sections = {s for s in args.sections.split(",") if s}
     n = args.n
     f64 = args.precision == "f64"
     evals = 10 if f64 else EVALS_PER_STEP
@@ -330,20 +626,26 @@ def run_mdsx(args):
     rng = np.random.default_rng(1000 + rank)
     pool_host = torch.from_numpy(rng.standard_normal((evals, n, P))).pin_memory()
     pool_dev = pool_host.to(f"cuda:{local}")
-    d_sum = torch.zeros(1, dtype=torch.float64, device=f"cuda:{local}")
+    d_sums = torch.zeros(evals, dtype=torch.float64, device=f"cuda:{local}")
+    check_idx = [0, evals // 2, evals - 1]
+    d_grads = torch.zeros((len(check_idx), n * P), dtype=torch.float64, device=f"cuda:{local}")
 
-    def device_step(events=None):
+    def device_step(events=None, keep=False):
         for k in range(evals):
             eng.update_locations_device(pool_dev[k].data_ptr())
             if events is not None:
                 events[k][0].record(stream)
-            eng.evaluate_device(d_sum.data_ptr(), None)
+            g = d_grads[check_idx.index(k)].data_ptr() if keep and k in check_idx else None
+            eng.evaluate_device(d_sums[k:k + 1].data_ptr(), g)
             if events is not None:
                 events[k][1].record(stream)
 
     torch.cuda.synchronize()
     for _ in range(args.warmup):
         device_step()
+    torch.cuda.synchronize()
+    d_sums.fill_(float("nan"))
+    d_grads.fill_(float("nan"))
     torch.cuda.synchronize()
 
     sampler = ClockSampler(local)
@@ -358,7 +660,7 @@ def run_mdsx(args):
     t0 = time.time()
     start.record(stream)
     for s in range(args.steps):
-        device_step(kev[s])
+        device_step(kev[s], keep=(s == args.steps - 1))
     stop.record(stream)
     torch.cuda.synchronize()
     t1 = time.time()
@@ -369,6 +671,8 @@ def run_mdsx(args):
     kernel_ms = statistics.mean(a.elapsed_time(b) for ev in kev for a, b in ev)
     launches = eng.last_launch_count()  # sweep launches per evaluation
     gpu_launches = args.steps * evals * (launches + 1)  # + the location conversion kernel
+    timed_sums = d_sums.cpu().numpy()
+    timed_grads = d_grads.cpu().numpy()
 
     elapsed_ms = across_ranks_max(elapsed_ms, world, f"cuda:{local}")
     value = job_throughput(args.steps * evals, world, elapsed_ms / 1000.0)
@@ -394,6 +698,7 @@ def run_mdsx(args):
     e2e_s = time.perf_counter() - t
     e2e_s = across_ranks_max(e2e_s, world, f"cuda:{local}")
     e2e_value = job_throughput(e2e_steps * evals, world, e2e_s)
+    eng.close()
 
     hbm_peak, peak_kind = peaks()
     bytes_per_launch = float(n) * n * 4 + 2.0 * n * P * 4
@@ -409,15 +714,16 @@ def run_mdsx(args):
 
     line = None
     if rank == 0:
-        x0 = pool_np[0]
-        cpu_v, cores, sample = cpu_port_sample(delta, x0, TAU, args.cpu_seconds)
+        cpu_s = cpu_port_full(delta, pool_np[0], TAU, os.cpu_count() or 1)
+        paths = cpu_paths(delta, pool_np[0], TAU, threaded_f64_value=1.0 / cpu_s, target_seconds=args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision, "data": DATA,
-            "config": {"workload": workload(n, args.precision, evals), "n": n, "p": P, "tau": TAU, "evals_per_step": evals,
-                       "schedule": args.schedule, "precision": args.precision,
-                       "delta_bytes": n * n * 4, "l2": f"inputs larger than L2 ({n * n * 4 / 1e9:.2f} GB delta vs 129 MB L2), no flush",
+            "config": {"workload": workload(n, args.precision, evals), "n": n, "p": P, "tau": TAU,
+                       "evals_per_step": evals, "schedule": args.schedule, "precision": args.precision,
+                       "delta_bytes": n * n * 4,
+                       "l2": f"inputs larger than L2 ({n * n * 4 / 1e9:.2f} GB delta vs 129 MB L2), no flush",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
@@ -428,9 +734,28 @@ def run_mdsx(args):
                     "d2h_bytes_per_step": evals * (n * P * 8 + 32)},
             "gpu_launches": gpu_launches,
             "clocks": sampler.summary(t0, t1),
-            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"one whole evaluation (all {n} rows: likelihood pass + gradient pass), "
+                                       f"{cpu_s:.2f} s", "paths": paths},
         }
-    eng.close()
+        if "parity" in sections or "f64" in sections:
+            xs = pool_np[check_idx]
+            refs = oracle_states(delta, xs, TAU)
+            if "parity" in sections:
+                tol_s = PARITY_TOL["f64_sum"] if f64 else PARITY_TOL["f32"]
+                tol_g = PARITY_TOL["f64_grad"] if f64 else PARITY_TOL["f32"]
+                line["parity"] = {
+                    "sum_rel_max": max(rel(float(timed_sums[k]), refs[m_][0]) for m_, k in enumerate(check_idx)),
+                    "grad_rel_max": max(grad_rel(timed_grads[m_], refs[m_][1]) for m_ in range(len(check_idx))),
+                    "evals_checked": len(check_idx), "of": "evaluations 0, 100 and 199 of the last timed step",
+                    "sums_finite": int(np.isfinite(timed_sums).sum()), "tolerance": [tol_s, tol_g]}
+            if "f64" in sections and not f64:
+                line["f64"] = measure_f64(local, delta, xs, refs)
+        del delta
+        if "c1" in sections:
+            line["c1"] = measure_c1(local, steps=5, warmup=3)
+        if "c3" in sections:
+            line["c3"] = measure_c3(local, steps=10, warmup=3)
     if world > 1:
         torch.distributed.destroy_process_group()
     if line is not None:
@@ -439,11 +764,19 @@ def run_mdsx(args):
 
 def main():
     args = parse()
-    if args.workload == "c1":
+    if args.workload in ("c1", "c3"):
+        rank, _, local = dist_env()
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the c1 workload's CPU time is its cpu_baseline"}))
-        else:
-            run_c1(args)
+            print(json.dumps({"impl": "reference",
+                              "unavailable": f"the {args.workload} workload's CPU time is its cpu_baseline"}))
+        elif rank == 0:
+            import torch
+
+            torch.cuda.set_device(local)
+            fn = measure_c1 if args.workload == "c1" else measure_c3
+            line = fn(local, steps=args.steps, warmup=args.warmup)
+            line.update({"n_gpus": 1, "scaling": "weak", "vs_baseline": None})
+            print(json.dumps(line), flush=True)
     elif args.impl == "reference":
         run_reference(args)
     else:

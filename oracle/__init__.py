@@ -13,9 +13,11 @@ never calls it.
 from .oracle import (  # noqa: F401
     ReferenceEngine,
     build,
+    evaluate,
     gradient,
     log_likelihood,
     port_eval_rows,
+    port_eval_rows_f32,
     reference_available,
     reference_root,
     sum_of_increments,

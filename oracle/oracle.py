@@ -6,6 +6,7 @@ is the reference engine built from its own sources by ``oracle/Makefile``.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 
@@ -73,6 +74,11 @@ def _oracle():
         ]
         lib.mdso_log_likelihood.restype = ctypes.c_double
         lib.mdso_log_likelihood.argtypes = [ctypes.c_double, ctypes.c_int64, ctypes.c_double]
+        lib.mdso_port_eval_rows_f32.restype = ctypes.c_double
+        lib.mdso_port_eval_rows_f32.argtypes = [
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_float, ctypes.c_int,
+            ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int,
+        ]
         lib.mdso_port_eval_rows.restype = ctypes.c_double
         lib.mdso_port_eval_rows.argtypes = [
             ctypes.c_void_p, ctypes.c_int, _dbl_p, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
@@ -135,6 +141,15 @@ def sweep_rows(delta, x, tau, truncation, row_begin, row_end, threads=None):
     return row_sum, grad
 
 
+def evaluate(delta, x, tau, truncation=True, threads=None):
+    """getSumOfIncrements() and getLogLikelihoodGradient() from one pass over
+    delta (the two calls above each sweep the whole matrix)."""
+    n = x.shape[0]
+    row_sum, grad = sweep_rows(delta, x, tau, truncation, 0, n, threads)
+    half = math.fsum(row_sum) / 2.0
+    return (half if truncation else 0.5 * tau * half), grad
+
+
 def log_likelihood(sum_of_incs: float, n: int, tau: float) -> float:
     """R/mds.R:24-28."""
     return _oracle().mdso_log_likelihood(float(sum_of_incs), int(n), float(tau))
@@ -149,6 +164,18 @@ def port_eval_rows(delta, x, tau, truncation, row_begin, row_end, threads=1):
     s = _oracle().mdso_port_eval_rows(d.ctypes.data, is32, x.ctypes.data_as(_dbl_p), n, p,
                                       float(tau), int(bool(truncation)), row_begin, row_end,
                                       grad.ctypes.data_as(_dbl_p), int(threads))
+    return s, grad
+
+
+def port_eval_rows_f32(delta32, x, tau, truncation, row_begin, row_end, threads=1):
+    """The reference FLOAT engine's per-evaluation work order over a row range
+    (single-precision CPU baseline timing); delta32 must be float32."""
+    d = np.ascontiguousarray(delta32, dtype=np.float32)
+    x32 = np.ascontiguousarray(x, dtype=np.float32)
+    n, p = x32.shape
+    grad = np.empty((row_end - row_begin, p), dtype=np.float32)
+    s = _oracle().mdso_port_eval_rows_f32(d.ctypes.data, x32.ctypes.data, n, p, float(tau), int(bool(truncation)),
+                                          row_begin, row_end, grad.ctypes.data, int(threads))
     return s, grad
 
 

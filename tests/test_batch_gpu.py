@@ -66,6 +66,34 @@ def test_mixed_instances_match_oracle():
         assert _rel(ll, oracle.log_likelihood(oracle.sum_of_increments(delta, x, tau), x.shape[0], tau)) < TOL
 
 
+def test_uneven_batch_at_full_scale_matches_oracle():
+    """Sixteen instances from the 64-instance workload's generator
+    (massivemds_gb300.batch_bench.make_instances: N ~ U{500..8000}, P cycling 2,
+    3, 6, tau ~ Gamma(2, 1), delta = distances of N points iid N(0, I_10),
+    FP32), the largest of them at N = 8000 so the top of the range is covered;
+    every instance against the FP64 oracle, with the tuned shapes and with the
+    default ones."""
+    from massivemds_gb300.batch_bench import make_instances
+
+    spec = make_instances(16, 3)
+    top = int(np.argmax([n for n, _, _, _ in spec]))
+    spec[top] = (8000,) + spec[top][1:]
+    problems = []
+    for n, p, tau, s in spec:
+        delta = gen.pairwise_distances(gen.latent_points(n, 10, s), dtype=np.float32)
+        x = np.random.default_rng(s + 1).standard_normal((n, p))
+        problems.append((delta, x, tau))
+    refs = [oracle.evaluate(delta, x, tau, True) for delta, x, tau in problems]
+    for tuned in (False, True):
+        with Batch() as b:
+            _fill(b, problems)
+            if tuned:
+                b.tune(repetitions=2)
+            for k, (s_ref, g_ref) in enumerate(refs):
+                assert _rel(b.getSumOfIncrements(k), s_ref) < TOL, (tuned, k, spec[k][:2])
+                assert _grad_rel(b.getLogLikelihoodGradient(k), g_ref) < TOL, (tuned, k, spec[k][:2])
+
+
 SHAPES = [(2, 1, 2), (2, 2, 1), (2, 4, 2), (3, 1, 1), (3, 2, 2), (3, 4, 1), (6, 1, 2), (6, 2, 1)]
 
 

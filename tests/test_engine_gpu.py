@@ -392,27 +392,8 @@ def test_device_api_matches_host_api():
 
 
 # ------------------------------------------------------------ full size (N=20k)
-
-@pytest.fixture(scope="module")
-def n20000():
-    n, p, tau = 20000, 2, 2.0
-    delta = gen.noisy_delta(n, dim=10, noise_sd=0.05, seed=666, dtype=np.float32)
-    x = gen.locations(n, p, seed=667)
-    return delta, x, tau, oracle.sum_of_increments(delta, x, tau), oracle.gradient(delta, x, tau)
-
-
-@pytest.mark.parametrize("mode", ["f32rows", "f32pairs", "f64s32rows", "f64s32pairs"])
-def test_full_size_n20000(mode, n20000):
-    """The N=20 000, P=2, tau=2 workload with FP32-stored delta: one evaluation
-    against the FP64 oracle on the same FP32 delta."""
-    delta, x, tau, s_ref, g_ref = n20000
-    n, p = x.shape
-    tol_s, tol_g = tolerances(mode)
-    e = make_engine(n, p, True, mode, delta, x, tau)
-    s, g = e.getSumOfIncrements(), e.getLogLikelihoodGradient()
-    e.close()
-    assert rel(s, s_ref) < tol_s
-    assert grad_rel(g, g_ref) < tol_g
+# tests/test_c2_full_gpu.py: the reference engine's golden vectors and twenty
+# oracle states at N = 20 000 in every precision mode.
 
 
 # ------------------------------------------------- bounded waits (failure path)

@@ -64,3 +64,28 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     with redirect_stdout(buf):
         bench.run_reference(args)
     assert buf.getvalue() == ""
+
+
+def test_reference_arm_line_reports_what_it_timed(monkeypatch):
+    """Rank 0 of the reference arm: one whole CPU evaluation per step, so
+    steps x ms_per_step fits inside the call's own wall time; the line carries
+    the host, the one-core and FP32 paths and the SIMD note."""
+    import json
+    import time
+
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    args = argparse.Namespace(n=96, steps=3, warmup=1, cpu_seconds=0.02, gpus=1, impl="reference")
+    buf = io.StringIO()
+    t = time.perf_counter()
+    with redirect_stdout(buf):
+        bench.run_reference(args)
+    wall_ms = 1000.0 * (time.perf_counter() - t)
+    line = json.loads(buf.getvalue())
+    assert line["impl"] == "reference" and line["config"]["evals_per_step"] == 1
+    assert line["steps"] * line["ms_per_step"] <= wall_ms
+    assert line["value"] == pytest.approx(1000.0 / line["ms_per_step"])
+    paths = line["cpu_baseline"]["paths"]
+    assert paths["serial_f64"]["cores"] == 1 and paths["threaded_f32"]["value"] > 0
+    assert paths["host"]["uname_m"] and "avx" in paths
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
