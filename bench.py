@@ -82,6 +82,10 @@ def parse():
     ap.add_argument("--workload", default="sweep", choices=["sweep", "c1", "c3"],
                     help="sweep: the headline N=20000 line (with f64, c1 and c3 sub-objects); c1: the reference's "
                          "benchmark case alone (N=1000, FP64, host API); c3: the 64-instance batch alone")
+    ap.add_argument("--partition", default="replicas", choices=["replicas", "rows"],
+                    help="multi-GPU: independent replicas of the workload (weak scaling, the default) or one "
+                         "problem split by rows of delta across the ranks (strong scaling, NCCL all-reduce of "
+                         "the sum and all-gather of the gradient rows every evaluation)")
     ap.add_argument("--cpu-seconds", type=float, default=3.0,
                     help="wall time of each bounded CPU row sample (one-core and FP32 paths)")
     ap.add_argument("--sections", default="parity,f64,c1,c3",
@@ -598,6 +602,87 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_partitioned(args):
+    """One N x N problem split by rows across the ranks (massivemds_gb300.partition):
+    rank r sweeps rows [r0, r1) of delta with an engine over those rows only
+    (row-block schedule, FP32, truncation); every rank holds the same
+    locations; per evaluation the ranks all-reduce the sum of increments and
+    all-gather the gradient rows (NCCL). value = whole-problem evals/s."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import massivemds_gb300 as m
+    from massivemds_gb300.partition import row_ranges
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    n, evals = args.n, EVALS_PER_STEP
+    ranges = row_ranges(n, world)
+    r0, r1 = ranges[rank]
+    width = max(b - a for a, b in ranges) * P
+    delta = make_delta(n)
+    eng = m.Engine(P, n, m.flags.FLOAT | m.flags.LEFT_TRUNCATION, local, rows=(r0, r1))
+    eng.setPairwiseData(delta[r0:r1])
+    eng.setParameters([TAU])
+    stream = torch.cuda.Stream(device=dev)
+    eng.set_stream(stream.cuda_stream)
+    pool = torch.from_numpy(np.random.default_rng(1000).standard_normal((evals, n, P))).to(dev)  # same on all ranks
+    d_sums = torch.zeros(evals, dtype=torch.float64, device=dev)
+    d_rows = torch.zeros(width, dtype=torch.float64, device=dev)
+    d_grad = torch.zeros(world * width, dtype=torch.float64, device=dev)
+
+    def step():
+        with torch.cuda.stream(stream):
+            for k in range(evals):
+                eng.update_locations_device(pool[k].data_ptr())
+                eng.evaluate_device(d_sums[k:k + 1].data_ptr(), d_rows.data_ptr())
+                dist.all_reduce(d_sums[k:k + 1])
+                dist.all_gather_into_tensor(d_grad, d_rows)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.5)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(args.steps):
+        step()
+    stop.record(stream)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    dist.barrier()
+    sampler.stop()
+    elapsed_ms = across_ranks_max(start.elapsed_time(stop), world, dev)
+    sums = d_sums.cpu().numpy()
+    grad = np.concatenate([d_grad[r * width:r * width + (b - a) * P].cpu().numpy() for r, (a, b) in enumerate(ranges)])
+    eng.close()
+    if rank == 0:
+        s_ref, g_ref = oracle_states(delta, pool[evals - 1:].cpu().numpy(), TAU)[0]
+        line = {
+            "metric": METRIC, "value": args.steps * evals / (elapsed_ms / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": {"workload": workload(n), "n": n, "p": P, "tau": TAU, "evals_per_step": evals,
+                       "parallelism": f"rows x{world} (delta rows split; NCCL all-reduce of the sum and all-gather "
+                                      "of the gradient per evaluation)",
+                       "rows_per_rank": [b - a for a, b in ranges], "delta_bytes_per_rank": (r1 - r0) * n * 4},
+            "parity": {"sum_rel": rel(float(sums[-1]), s_ref), "grad_rel": grad_rel(grad, g_ref),
+                       "evals_checked": 1, "tolerance": PARITY_TOL["f32"]},
+            "gpu_launches": args.steps * evals * 2,
+            "clocks": sampler.summary(t0, t1),
+        }
+        print(json.dumps(line), flush=True)
+    dist.destroy_process_group()
+
+
 def run_mdsx(args):
     import numpy as np
     import torch
@@ -779,6 +864,8 @@ def main():
             print(json.dumps(line), flush=True)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.partition == "rows":
+        run_partitioned(args)
     else:
         run_mdsx(args)
 

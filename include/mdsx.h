@@ -62,6 +62,25 @@ typedef struct mdsx_engine mdsx_engine;
 int mdsx_create(int embedding_dimension, int location_count, long flags, int device,
                 mdsx_engine** out);
 
+/* A row range of one problem, for splitting a sweep across GPUs: the engine
+ * holds and sweeps rows [row_begin, row_end) of the N x N delta only. This is
+ * the reference's own parallel split -- its TBB engine partitions the rows i
+ * of both passes (parallel_reduce / parallel_for over i,
+ * src/NewMultiDimensionalScaling.hpp:708-744) -- across devices instead of
+ * threads. Differences from mdsx_create: setPairwiseData takes the range's
+ * rows, (row_end - row_begin) * N values; updateLocations still takes all N
+ * locations; getSumOfIncrements returns the range's share (the sum over
+ * ranges is the whole matrix's value); getLogLikelihood the range's share of
+ * R/mds.R:24-28 (observation count (row_end - row_begin)(N - 1)/2);
+ * getLogLikelihoodGradient the range's rows, (row_end - row_begin) * P values
+ * (row i of the gradient reads only row i of delta, :421-461). Row ranges use
+ * the row-block schedule; the HMC driver and the surrogate need a whole-matrix
+ * engine. */
+int mdsx_create_rows(int embedding_dimension, int location_count, long flags, int device, int row_begin,
+                     int row_end, mdsx_engine** out);
+/* [row_begin, row_end) of an engine: [0, N) unless made by mdsx_create_rows. */
+int mdsx_get_row_range(const mdsx_engine* engine, int* row_begin, int* row_end);
+
 /* Replaces the engine destructor (src/NewMultiDimensionalScaling.hpp:130). */
 int mdsx_destroy(mdsx_engine* engine);
 

@@ -29,6 +29,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _i, _sz, _l = ctypes.c_int, ctypes.c_size_t, ctypes.c_long
 SIGNATURES = {
     "mdsx_create": (_i, [_i, _i, _l, _i, ctypes.POINTER(_vp)]),
+    "mdsx_create_rows": (_i, [_i, _i, _l, _i, _i, _i, ctypes.POINTER(_vp)]),
+    "mdsx_get_row_range": (_i, [_vp, _ip, _ip]),
     "mdsx_destroy": (_i, [_vp]),
     "mdsx_update_locations": (_i, [_vp, _i, _dp, _sz]),
     "mdsx_get_sum_of_increments": (_i, [_vp, _dp]),

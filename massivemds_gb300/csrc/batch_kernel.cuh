@@ -222,9 +222,9 @@ __global__ void __launch_bounds__(kThreads, MDSX_F32_MIN_CTAS) batch_sweep_kerne
             const float* dtile = sdelta + stage * (RB * kStepCols) + (warp * RW) * kStepCols + 4 * lane;
             const float* xtile = sx + stage * (P * kStepCols) + 4 * lane;
             if (masked)
-                stage_f32<P, TRUNC, true, RW>(dtile, xtile, xi2, row0, j0, n, lane, kc, g2, r2p, prodp);
+                stage_f32<P, TRUNC, true, RW>(dtile, xtile, xi2, row0, j0, n, n, lane, kc, g2, r2p, prodp);
             else
-                stage_f32<P, TRUNC, false, RW>(dtile, xtile, xi2, row0, j0, n, lane, kc, g2, r2p, prodp);
+                stage_f32<P, TRUNC, false, RW>(dtile, xtile, xi2, row0, j0, n, n, lane, kc, g2, r2p, prodp);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[stage]);
             if (++stage == kStages) {

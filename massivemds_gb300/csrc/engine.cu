@@ -167,7 +167,7 @@ int plan_and_allocate(mdsx_engine* e) {
     MDSX_CUDA(e, mdsx::sweep_occupancy(e->mode, e->p, e->trunc, &ctas));
     if (ctas < 1) return fail(e, MDSX_ECUDA, "sweep kernel cannot be resident on this device");
     const int rb = e->shape.rb;
-    e->n_row_blocks = (e->n + rb - 1) / rb;
+    e->n_row_blocks = (e->rows + rb - 1) / rb;
     e->rows_padded = e->n_row_blocks * rb;
     // Stream-K partition: U = row blocks x 128-column stages, split evenly
     // over G <= U CTAs (so no CTA has an empty range).
@@ -184,19 +184,19 @@ int plan_and_allocate(mdsx_engine* e) {
 
     const int delta_elem = e->shape.delta_elem_bytes;
     e->ld = round_up(e->n, 16 / delta_elem);
-    e->x_ld = (int)std::max<long long>(round_up(e->n, mdsx::kStepCols), e->rows_padded);
+    e->x_ld = (int)std::max<long long>(round_up(e->n, mdsx::kStepCols), (long long)e->row_begin + e->rows_padded);
     // P location rows and one flag row (read by the unordered-pair schedule)
     const size_t x_bytes = (size_t)(e->p + 1) * e->x_ld * e->shape.x_elem_bytes;
     const size_t acc_bytes = e->x_f32 ? 4 : 8;
 
-    MDSX_CUDA(e, cudaMalloc(&e->d_delta, (size_t)e->n * e->ld * delta_elem));
+    MDSX_CUDA(e, cudaMalloc(&e->d_delta, (size_t)e->rows * e->ld * delta_elem));
     MDSX_CUDA(e, cudaMalloc(&e->d_x[0], x_bytes));
     MDSX_CUDA(e, cudaMalloc(&e->d_x[1], x_bytes));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_x[0], 0, x_bytes, e->stream));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_x[1], 0, x_bytes, e->stream));
     MDSX_CUDA(e, cudaMalloc(&e->d_xin, (size_t)e->n * e->p * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_grad[0], (size_t)e->n * e->p * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_grad[1], (size_t)e->n * e->p * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_grad[0], (size_t)e->rows * e->p * sizeof(double)));
+    MDSX_CUDA(e, cudaMalloc(&e->d_grad[1], (size_t)e->rows * e->p * sizeof(double)));
     MDSX_CUDA(e, cudaMalloc(&e->d_out, 4 * sizeof(double)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_out, 0, 4 * sizeof(double), e->stream));
     MDSX_CUDA(e, cudaMalloc(&e->d_gpart, (size_t)e->n_row_blocks * e->max_slots * rb * e->p * acc_bytes));
@@ -209,13 +209,14 @@ int plan_and_allocate(mdsx_engine* e) {
     MDSX_CUDA(e, cudaMemsetAsync(e->d_row_nan, 0, (size_t)e->rows_padded * sizeof(int), e->stream));
     MDSX_CUDA(e, cudaMallocHost(&e->h_out, 4 * sizeof(double)));
 
-    int rc = make_tmap_2d(e, &e->tmap_delta, e->d_delta, e->delta_f32, e->n, e->n, e->ld, mdsx::kStepCols, rb);
+    int rc = make_tmap_2d(e, &e->tmap_delta, e->d_delta, e->delta_f32, e->n, e->rows, e->ld, mdsx::kStepCols, rb);
     if (rc) return rc;
     for (int b = 0; b < 2; ++b) {
         rc = make_tmap_2d(e, &e->tmap_x[b], e->d_x[b], e->x_f32, e->n, e->p, e->x_ld, mdsx::kStepCols, e->p);
         if (rc) return rc;
     }
-    if (mdsx::pair_built(e->mode, e->p)) {
+    // The unordered-pair schedule needs both delta_ij and delta_ji: whole-matrix engines only.
+    if (mdsx::pair_built(e->mode, e->p) && e->rows == e->n) {
         rc = plan_pairs(e);
         if (rc) return rc;
         // Measured on GB300: with truncation the pair math dominates and sharing it between
@@ -231,6 +232,7 @@ int plan_and_allocate(mdsx_engine* e) {
 
 // Flag row (row P) of both location buffers from the NaN-row marks.
 cudaError_t write_flags(mdsx_engine* e) {
+    if (e->rows != e->n) return cudaSuccess;  // the flag row serves the unordered-pair schedule only
     const size_t elem = e->x_f32 ? sizeof(float) : sizeof(double);
     for (int b = 0; b < 2; ++b) {
         cudaError_t err = mdsx::write_flag_row(e->d_row_nan, e->n, e->rows_padded,
@@ -251,6 +253,8 @@ void reset_scratch(mdsx_engine* e) {
 SweepArgs make_args(mdsx_engine* e) {
     SweepArgs a{};
     a.n = e->n;
+    a.row_offset = e->row_begin;
+    a.rows = e->rows;
     a.n_row_blocks = e->n_row_blocks;
     a.steps_per_row = e->steps_per_row;
     a.grid = e->grid;
@@ -387,7 +391,8 @@ extern "C" {
 
 const char* mdsx_version(void) { return "mdsx 0.1 (sm_103a)"; }
 
-int mdsx_create(int embedding_dimension, int location_count, long flags, int device, mdsx_engine** out) {
+int mdsx_create_rows(int embedding_dimension, int location_count, long flags, int device, int row_begin, int row_end,
+                     mdsx_engine** out) {
     if (!out) return fail(nullptr, MDSX_EINVAL, "out is NULL");
     *out = nullptr;
     if (embedding_dimension < 1) return fail(nullptr, MDSX_EINVAL, "embeddingDimension must be >= 1");
@@ -395,6 +400,8 @@ int mdsx_create(int embedding_dimension, int location_count, long flags, int dev
         return fail(nullptr, MDSX_EUNSUPPORTED, "embeddingDimension above MDSX_MAX_DIMENSION");
     if (location_count < 1) return fail(nullptr, MDSX_EINVAL, "locationCount must be >= 1");
     if (location_count > (1 << 20)) return fail(nullptr, MDSX_EINVAL, "locationCount above 2^20");
+    if (row_begin < 0 || row_end > location_count || row_begin >= row_end)
+        return fail(nullptr, MDSX_EINVAL, "row range must satisfy 0 <= row_begin < row_end <= locationCount");
     int count = 0;
     cudaError_t err = cudaGetDeviceCount(&count);
     if (err != cudaSuccess || count == 0)
@@ -407,6 +414,8 @@ int mdsx_create(int embedding_dimension, int location_count, long flags, int dev
     auto* e = new mdsx_engine;
     e->p = embedding_dimension;
     e->n = location_count;
+    e->row_begin = row_begin;
+    e->rows = row_end - row_begin;
     e->flags = flags;
     e->device = device;
     e->trunc = (flags & MDSX_FLAG_LEFT_TRUNCATION) != 0;
@@ -438,6 +447,17 @@ int mdsx_create(int embedding_dimension, int location_count, long flags, int dev
         return rc;
     }
     *out = e;
+    return MDSX_OK;
+}
+
+int mdsx_create(int embedding_dimension, int location_count, long flags, int device, mdsx_engine** out) {
+    return mdsx_create_rows(embedding_dimension, location_count, flags, device, 0, location_count, out);
+}
+
+int mdsx_get_row_range(const mdsx_engine* e, int* row_begin, int* row_end) {
+    if (!e || !row_begin || !row_end) return MDSX_EINVAL;
+    *row_begin = e->row_begin;
+    *row_end = e->row_begin + e->rows;
     return MDSX_OK;
 }
 
@@ -495,7 +515,8 @@ int mdsx_get_sum_of_increments(mdsx_engine* e, double* out) {
 int mdsx_get_log_likelihood_gradient(mdsx_engine* e, double* out, size_t length) {
     if (!e) return MDSX_EINVAL;
     if (!out) return fail(e, MDSX_EINVAL, "out is NULL");
-    if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "getLogLikelihoodGradient: length != N*P");
+    if (length != (size_t)e->rows * e->p)
+        return fail(e, MDSX_EINVAL, "getLogLikelihoodGradient: length != N*P (rows*P for a row range)");
     DeviceGuard guard(e->device);
     if (!e->grad_known) {
         int rc = sweep_and_read(e);
@@ -514,8 +535,8 @@ int mdsx_store_state(mdsx_engine* e) {
     MDSX_CUDA(e, cudaMemcpyAsync(e->d_x[other], e->d_x[e->xcur], x_bytes, cudaMemcpyDeviceToDevice, e->stream));
     e->stored_grad_known = e->grad_known;
     if (e->grad_known)
-        MDSX_CUDA(e, cudaMemcpyAsync(e->d_grad[1 - e->gcur], e->d_grad[e->gcur], (size_t)e->n * e->p * sizeof(double),
-                                     cudaMemcpyDeviceToDevice, e->stream));
+        MDSX_CUDA(e, cudaMemcpyAsync(e->d_grad[1 - e->gcur], e->d_grad[e->gcur],
+                                     (size_t)e->rows * e->p * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     e->stored_sum_r2 = e->sum_r2;
     e->stored_sum_log = e->sum_log;
     e->stored_tau = e->tau;
@@ -540,7 +561,8 @@ int mdsx_accept_state(mdsx_engine* e) { return e ? MDSX_OK : MDSX_EINVAL; }
 int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
     if (!e) return MDSX_EINVAL;
     if (!data) return fail(e, MDSX_EINVAL, "data pointer is NULL");
-    if (length != (size_t)e->n * e->n) return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N");
+    if (length != (size_t)e->rows * e->n)
+        return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N (rows*N for a row range)");
     DeviceGuard guard(e->device);
     if (!e->delta_f32 && e->ld == e->n) {
         MDSX_CUDA(e, cudaMemcpyAsync(e->d_delta, data, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
@@ -549,10 +571,10 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
         const long long chunk_elems = 16LL << 20;  // 128 MB of doubles
         const long long rows_per_chunk = std::max(1LL, chunk_elems / e->n);
         double* staging = nullptr;
-        MDSX_CUDA(e, cudaMalloc(&staging, (size_t)std::min<long long>(rows_per_chunk, e->n) * e->n * sizeof(double)));
+        MDSX_CUDA(e, cudaMalloc(&staging, (size_t)std::min<long long>(rows_per_chunk, e->rows) * e->n * sizeof(double)));
         const int elem = e->delta_f32 ? 4 : 8;
-        for (long long r0 = 0; r0 < e->n; r0 += rows_per_chunk) {
-            const long long rows = std::min<long long>(rows_per_chunk, e->n - r0);
+        for (long long r0 = 0; r0 < e->rows; r0 += rows_per_chunk) {
+            const long long rows = std::min<long long>(rows_per_chunk, e->rows - r0);
             cudaError_t err = cudaMemcpyAsync(staging, data + r0 * e->n, (size_t)(rows * e->n) * sizeof(double),
                                               cudaMemcpyHostToDevice, e->stream);
             if (err == cudaSuccess)
@@ -567,7 +589,8 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
         }
         cudaFree(staging);
     }
-    MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, e->delta_f32, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+    MDSX_CUDA(e, mdsx::mark_nan_rows_block(e->d_delta, e->delta_f32, e->rows, e->n, e->ld, e->d_row_nan,
+                                           e->rows_padded, e->stream));
     MDSX_CUDA(e, write_flags(e));
     MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
     e->data_set = true;
@@ -578,12 +601,15 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
 int mdsx_set_pairwise_data_f32(mdsx_engine* e, const float* data, size_t length) {
     if (!e) return MDSX_EINVAL;
     if (!data) return fail(e, MDSX_EINVAL, "data pointer is NULL");
-    if (length != (size_t)e->n * e->n) return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N");
+    if (length != (size_t)e->rows * e->n)
+        return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N (rows*N for a row range)");
     DeviceGuard guard(e->device);
     if (e->delta_f32) {
         MDSX_CUDA(e, cudaMemcpy2DAsync(e->d_delta, (size_t)e->ld * sizeof(float), data, (size_t)e->n * sizeof(float),
-                                       (size_t)e->n * sizeof(float), (size_t)e->n, cudaMemcpyHostToDevice, e->stream));
-        MDSX_CUDA(e, mdsx::mark_nan_rows(e->d_delta, true, e->n, e->ld, e->d_row_nan, e->rows_padded, e->stream));
+                                       (size_t)e->n * sizeof(float), (size_t)e->rows, cudaMemcpyHostToDevice,
+                                       e->stream));
+        MDSX_CUDA(e, mdsx::mark_nan_rows_block(e->d_delta, true, e->rows, e->n, e->ld, e->d_row_nan, e->rows_padded,
+                                               e->stream));
         MDSX_CUDA(e, write_flags(e));
         MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
         e->data_set = true;
@@ -630,7 +656,8 @@ int mdsx_get_log_likelihood(mdsx_engine* e, double* out) {
     double s = 0.0;
     int rc = mdsx_get_sum_of_increments(e, &s);
     if (rc) return rc;
-    const double observation_count = (double)e->n * (double)(e->n - 1) / 2.0;
+    // R/mds.R:24-28; a row range carries its rows' share of the N(N-1)/2 observations.
+    const double observation_count = (double)e->rows * (double)(e->n - 1) / 2.0;
     *out = 0.5 * (std::log(e->tau) - std::log(2.0 * M_PI)) * observation_count - s;
     return MDSX_OK;
 }
@@ -663,7 +690,7 @@ int mdsx_evaluate_device(mdsx_engine* e, double* d_sum, double* d_gradient) {
     if (d_sum)
         MDSX_CUDA(e, cudaMemcpyAsync(d_sum, e->d_out + 2, sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
     if (d_gradient)
-        MDSX_CUDA(e, cudaMemcpyAsync(d_gradient, e->d_grad[e->gcur], (size_t)e->n * e->p * sizeof(double),
+        MDSX_CUDA(e, cudaMemcpyAsync(d_gradient, e->d_grad[e->gcur], (size_t)e->rows * e->p * sizeof(double),
                                      cudaMemcpyDeviceToDevice, e->stream));
     e->last_launches = launches;
     // Results live on the device; the host-side cache is refreshed lazily.
@@ -676,6 +703,8 @@ int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
     if (!e) return MDSX_EINVAL;
     if (schedule != MDSX_SWEEP_ROWS && schedule != MDSX_SWEEP_PAIRS)
         return fail(e, MDSX_EINVAL, "unknown sweep schedule");
+    if (schedule == MDSX_SWEEP_PAIRS && e->rows != e->n)
+        return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule needs an engine over the whole matrix");
     if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
         return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for P <= 6 only");
     if (schedule != e->schedule) {

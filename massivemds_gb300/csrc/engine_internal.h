@@ -17,6 +17,9 @@ using mdsx::SweepArgs;
 
 struct mdsx_engine {
     int p = 0, n = 0;
+    // Rows of delta this engine holds and sweeps: [row_begin, row_begin + rows).
+    // The whole matrix (row_begin 0, rows N) unless made by mdsx_create_rows.
+    int row_begin = 0, rows = 0;
     long flags = 0;
     int device = 0;
     bool trunc = false;

@@ -178,6 +178,8 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
 
     mdsx::SweepArgs a{};
     a.n = n;
+    a.row_offset = 0;
+    a.rows = n;
     a.n_row_blocks = n_row_blocks;
     a.steps_per_row = steps_per_row;
     a.grid = grid;

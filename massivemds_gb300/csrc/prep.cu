@@ -52,15 +52,15 @@ __global__ void copy_delta_rows_f32_kernel(const float* __restrict__ src, long l
 
 // One warp per row.
 template <typename T>
-__global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int n, long long ld, int* __restrict__ row_nan,
-                                     int rows_padded) {
+__global__ void mark_nan_rows_kernel(const T* __restrict__ delta, int rows, int cols, long long ld,
+                                     int* __restrict__ row_nan, int rows_padded) {
     const int warps = (gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
     for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < rows_padded; row += warps) {
         int bad = 0;
-        if (row < n) {
+        if (row < rows) {
             const T* r = delta + (long long)row * ld;
-            for (int c = lane; c < n; c += 32) bad |= (r[c] != r[c]);
+            for (int c = lane; c < cols; c += 32) bad |= (r[c] != r[c]);
             bad = __any_sync(0xffffffffu, bad);
         } else {
             bad = 1;
@@ -122,15 +122,21 @@ cudaError_t copy_delta_rows_f32(const float* src, long long rows, int n, float* 
     return cudaGetLastError();
 }
 
-cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, int* row_nan, int rows_padded,
-                          cudaStream_t s) {
+cudaError_t mark_nan_rows_block(const void* delta, bool is_f32, int rows, int cols, long long ld, int* row_nan,
+                                int rows_padded, cudaStream_t s) {
     const int grid = grid_for((long long)rows_padded * 32, 256);
     if (is_f32)
-        mark_nan_rows_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(delta), n, ld, row_nan, rows_padded);
+        mark_nan_rows_kernel<float><<<grid, 256, 0, s>>>(static_cast<const float*>(delta), rows, cols, ld, row_nan,
+                                                         rows_padded);
     else
-        mark_nan_rows_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(delta), n, ld, row_nan,
+        mark_nan_rows_kernel<double><<<grid, 256, 0, s>>>(static_cast<const double*>(delta), rows, cols, ld, row_nan,
                                                           rows_padded);
     return cudaGetLastError();
+}
+
+cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, int* row_nan, int rows_padded,
+                          cudaStream_t s) {
+    return mark_nan_rows_block(delta, is_f32, n, n, ld, row_nan, rows_padded, s);
 }
 
 cudaError_t mark_padding_rows(int n, int* row_nan, int rows_padded, cudaStream_t s) {

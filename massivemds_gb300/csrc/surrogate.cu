@@ -424,6 +424,7 @@ int mdsx_surrogate_create(mdsx_engine* e, int landmarks, int hidden_width, int h
     if (hidden_layers < 1 || hidden_layers > 8) return fail(e, MDSX_EINVAL, "surrogate: 1..8 hidden layers");
     if (max_rows < 64) return fail(e, MDSX_EINVAL, "surrogate: max_rows must be >= 64");
     if (!e->data_set) return fail(e, MDSX_ESTATE, "surrogate: setPairwiseData has not been called");
+    if (e->rows != e->n) return fail(e, MDSX_EUNSUPPORTED, "surrogate: needs an engine over the whole matrix");
     mdsx::internal::DeviceGuard guard(e->device);
     auto* s = new mdsx_surrogate;
     s->engine = e;

@@ -83,6 +83,9 @@ cudaError_t copy_delta_rows_f32(const float* src, long long rows, int n, float* 
 // row_nan[i] = 1 if row i (< n) has a NaN in columns [0, n); rows in [n, rows_padded) get 1.
 cudaError_t mark_nan_rows(const void* delta, bool is_f32, int n, long long ld, int* row_nan, int rows_padded,
                           cudaStream_t s);
+// The same over a block of `rows` rows of `cols` columns (a row partition of delta).
+cudaError_t mark_nan_rows_block(const void* delta, bool is_f32, int rows, int cols, long long ld, int* row_nan,
+                                int rows_padded, cudaStream_t s);
 // row_nan[i] = 0 for rows < n and 1 for rows in [n, rows_padded), without reading delta.
 cudaError_t mark_padding_rows(int n, int* row_nan, int rows_padded, cudaStream_t s);
 

@@ -60,16 +60,18 @@ constexpr int kLogFoldPairs = 64;
 constexpr int kLogFoldF64Stages = 64;  // FP64: 256 factors >= 1/2 per product stay above 1e-78                    // product of <= 64 factors in [1, 2] cannot overflow
 
 struct SweepArgs {
-    int n;               // locations N
-    int n_row_blocks;    // ceil(N / RB)
+    int n;               // locations N (the columns of delta)
+    int row_offset;      // first row of delta this launch covers (a row partition; 0 for the whole matrix)
+    int rows;            // rows covered: [row_offset, row_offset + rows); N for the whole matrix
+    int n_row_blocks;    // ceil(rows / RB)
     int steps_per_row;   // S = ceil(N / 128): units per row block
     int grid;            // G: CTAs launched (<= U, so no CTA has an empty range)
     long long n_units;   // U = n_row_blocks * S
     int max_slots;       // most CTAs meeting one row block
     int rows_padded;     // n_row_blocks * RB
-    int x_ld;            // row stride of the SoA location array [P][x_ld]
+    int x_ld;            // row stride of the SoA location array [P][x_ld], >= row_offset + rows_padded
     const void* x;       // SoA locations (compute type)
-    const int* row_nan;  // [rows_padded]; nonzero: row has a NaN, or row >= N
+    const int* row_nan;  // [rows_padded], by covered row; nonzero: row has a NaN, or lies past the covered rows
     // FP32 pair constants (d-space): E' = 2^(d^2 k_e + log2_k2) = exp(-tau d^2/2)/sqrt(2 pi tau)
     float k_e, log2_k2;
     float tp0, tp1, tp2, ts0, ts1, ts2;  // 1/Phi = S(d) / (S(d) - E' P(d))
@@ -81,7 +83,7 @@ struct SweepArgs {
     unsigned* rb_count;    // [n_row_blocks] warp publications per row block
     unsigned* done_count;  // [1] completed row blocks
     // outputs
-    double* grad_out;  // [N][P] = tau * sum_j ..., row-major
+    double* grad_out;  // [rows][P] = tau * sum_j ..., row-major, covered rows only
     double* sums_out;  // [0] = sum of r^2, [1] = sum of logPhi, over ordered non-missing pairs,
                        // [2] = getSumOfIncrements() of those sums
     int truncation;
@@ -271,7 +273,7 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
 // and one 1/Phi product pack per lane keep the register budget.
 template <int P, bool TRUNC, bool MASKED, int RW>
 __device__ __forceinline__ void stage_f32(const float* __restrict__ dtile, const float* __restrict__ xtile,
-                                          const f2 (&xi)[RW][P], int i0, int j0, int n, int lane,
+                                          const f2 (&xi)[RW][P], int i0, int j0, int n, int i_lim, int lane,
                                           const PairConstsF32& kc, f2 (&g)[RW][P], f2& r2, f2& prod) {
     f2 xj[2][P];
 #pragma unroll
@@ -296,8 +298,8 @@ __device__ __forceinline__ void stage_f32(const float* __restrict__ dtile, const
                 float a, b;
                 upk(dl[r][h], a, b);
                 const int i = i0 + r, j = j0 + 4 * lane + 2 * h;
-                v0 = (j < n) && (i < n) && (i != j) && (a == a);
-                v1 = (j + 1 < n) && (i < n) && (i != j + 1) && (b == b);
+                v0 = (j < n) && (i < i_lim) && (i != j) && (a == a);
+                v1 = (j + 1 < n) && (i < i_lim) && (i != j + 1) && (b == b);
             }
             pair2_f32<P, TRUNC, MASKED>(xi[r], xj[h], dl[r][h], v0, v1, kc, g[r], r2, prod);
         }
@@ -306,7 +308,8 @@ __device__ __forceinline__ void stage_f32(const float* __restrict__ dtile, const
 
 template <int P, bool TRUNC, bool MASKED, int RW, typename S>
 __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const double* __restrict__ xtile,
-                                          const double (&xi)[RW][P], int i0, int j0, int n, int lane, double tau,
+                                          const double (&xi)[RW][P], int i0, int j0, int n, int i_lim, int lane,
+                                          double tau,
                                           double sqrt_tau, double (&g)[RW][P], double (&r2)[RW],
                                           double (&lprod)[RW]) {
     double xj[P][4];
@@ -332,7 +335,7 @@ __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const dou
             bool valid = true;
             if (MASKED) {
                 const int i = i0 + r, j = j0 + 4 * lane + c;
-                valid = (j < n) && (i < n) && (i != j) && (dl[c] == dl[c]);
+                valid = (j < n) && (i < i_lim) && (i != j) && (dl[c] == dl[c]);
             }
             pair_f64<P, TRUNC, MASKED>(xi[r], xj, c, dl[c], valid, tau, sqrt_tau, g[r], r2[r], lprod[r]);
         }
@@ -467,7 +470,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
         const int n_slots = cta_of_unit(rb_end - 1, a.n_units, a.grid) - first_cta + 1;
         const int slot = blockIdx.x - first_cta;
         u = seg_end;
-        const int row0 = rb * RB + warp * RW;
+        const int row0 = rb * RB + warp * RW;     // covered-row index (row marks, partials, output)
+        const int grow0 = a.row_offset + row0;     // row of the whole matrix (diagonal, locations)
+        const int i_lim = a.row_offset + a.rows;
 
         C xi[RW][P];
         f2 xi2[RW][P];  // FP32: (x_i, x_i) packs
@@ -478,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
             rows_clean &= (a.row_nan[i] == 0);
 #pragma unroll
             for (int q = 0; q < P; ++q) {
-                xi[r][q] = xg[(size_t)q * a.x_ld + i];
+                xi[r][q] = xg[(size_t)q * a.x_ld + a.row_offset + i];
                 if constexpr (F32) xi2[r][q] = pk(xi[r][q], xi[r][q]);
             }
         }
@@ -510,20 +515,20 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                 break;
             }
             const int j0 = (st0 + s) * kStepCols;
-            const bool masked = !rows_clean || (j0 + kStepCols > a.n) || (j0 < row0 + RW && row0 < j0 + kStepCols);
+            const bool masked = !rows_clean || (j0 + kStepCols > a.n) || (j0 < grow0 + RW && grow0 < j0 + kStepCols);
             const S* dtile = sdelta + stage * (RB * kStepCols) + (warp * RW) * kStepCols + 4 * lane;
             const C* xtile = sx + stage * (P * kStepCols) + 4 * lane;
             if constexpr (F32) {
                 if (masked)
-                    stage_f32<P, TRUNC, true, RW>(dtile, xtile, xi2, row0, j0, a.n, lane, kc, g2, r2p, prodp);
+                    stage_f32<P, TRUNC, true, RW>(dtile, xtile, xi2, grow0, j0, a.n, i_lim, lane, kc, g2, r2p, prodp);
                 else
-                    stage_f32<P, TRUNC, false, RW>(dtile, xtile, xi2, row0, j0, a.n, lane, kc, g2, r2p, prodp);
+                    stage_f32<P, TRUNC, false, RW>(dtile, xtile, xi2, grow0, j0, a.n, i_lim, lane, kc, g2, r2p, prodp);
             } else {
                 if (masked)
-                    stage_f64<P, TRUNC, true, RW>(dtile, xtile, xi, row0, j0, a.n, lane, a.tau, a.sqrt_tau, g, r2,
+                    stage_f64<P, TRUNC, true, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.tau, a.sqrt_tau, g, r2,
                                                   prod64);
                 else
-                    stage_f64<P, TRUNC, false, RW>(dtile, xtile, xi, row0, j0, a.n, lane, a.tau, a.sqrt_tau, g,
+                    stage_f64<P, TRUNC, false, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.tau, a.sqrt_tau, g,
                                                    r2, prod64);
             }
             __syncwarp();
@@ -628,7 +633,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                 sum += (double)__ldcg(&gpart[(((size_t)rb * a.max_slots + k) * RB + rr) * P + q]);
             const int row = rb * RB + rr;
             // FP32 partials hold the negated gradient terms.
-            if (row < a.n) a.grad_out[(size_t)row * P + q] = (F32 ? -a.tau : a.tau) * sum;
+            if (row < a.rows) a.grad_out[(size_t)row * P + q] = (F32 ? -a.tau : a.tau) * sum;
         }
         double br2 = 0.0, blog = 0.0;
         for (int idx = lane; idx < n_slots * kConsumerWarps; idx += 32) {

@@ -27,15 +27,26 @@ _dp = ctypes.POINTER(ctypes.c_double)
 class Engine:
     """A GPU MDS engine: ``mds::AbstractMultiDimensionalScaling`` through libmdsx.so."""
 
-    def __init__(self, embeddingDimension: int, locationCount: int, flags: int = 0, device: int = -1):
+    def __init__(self, embeddingDimension: int, locationCount: int, flags: int = 0, device: int = -1,
+                 rows: tuple[int, int] | None = None):
+        """``rows=(row_begin, row_end)`` makes an engine over those rows of delta
+        only (mdsx_create_rows): setPairwiseData then takes the rows' (row_end -
+        row_begin) x N values, getSumOfIncrements / getLogLikelihood return the
+        rows' share and getLogLikelihoodGradient their gradient rows."""
         self._lib = load()
         h = ctypes.c_void_p()
-        check(self._lib.mdsx_create(int(embeddingDimension), int(locationCount), int(flags), int(device),
-                                    ctypes.byref(h)))
+        if rows is None:
+            check(self._lib.mdsx_create(int(embeddingDimension), int(locationCount), int(flags), int(device),
+                                        ctypes.byref(h)))
+            rows = (0, int(locationCount))
+        else:
+            check(self._lib.mdsx_create_rows(int(embeddingDimension), int(locationCount), int(flags), int(device),
+                                             int(rows[0]), int(rows[1]), ctypes.byref(h)))
         self._h = h
         self.embeddingDimension = int(embeddingDimension)
         self.locationCount = int(locationCount)
         self.flags = int(flags)
+        self.rowBegin, self.rowEnd = int(rows[0]), int(rows[1])
 
     # -- lifetime
     def close(self) -> None:
@@ -69,11 +80,11 @@ class Engine:
         return out.value
 
     def getLogLikelihoodGradient(self, out: np.ndarray | None = None) -> np.ndarray:
-        n = self.locationCount * self.embeddingDimension
+        n = (self.rowEnd - self.rowBegin) * self.embeddingDimension
         if out is None:
             out = np.empty(n, dtype=np.float64)
         if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != n:
-            raise ValueError("gradient buffer must be a contiguous float64 array of N*P entries")
+            raise ValueError("gradient buffer must be a contiguous float64 array of N*P entries (rows*P for a row range)")
         self._check(self._lib.mdsx_get_log_likelihood_gradient(self._h, out.ctypes.data_as(_dp), out.size))
         return out
 
