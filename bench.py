@@ -661,6 +661,7 @@ def run_partitioned(args):
     dist.barrier()
     sampler.stop()
     elapsed_ms = across_ranks_max(start.elapsed_time(stop), world, dev)
+    launches = eng.last_launch_count()
     sums = d_sums.cpu().numpy()
     grad = np.concatenate([d_grad[r * width:r * width + (b - a) * P].cpu().numpy() for r, (a, b) in enumerate(ranges)])
     eng.close()
@@ -676,7 +677,7 @@ def run_partitioned(args):
                        "rows_per_rank": [b - a for a, b in ranges], "delta_bytes_per_rank": (r1 - r0) * n * 4},
             "parity": {"sum_rel": rel(float(sums[-1]), s_ref), "grad_rel": grad_rel(grad, g_ref),
                        "evals_checked": 1, "tolerance": PARITY_TOL["f32"]},
-            "gpu_launches": args.steps * evals * 2,
+            "gpu_launches": args.steps * evals * (launches + 1),  # sweep kernels + the location conversion
             "clocks": sampler.summary(t0, t1),
         }
         print(json.dumps(line), flush=True)

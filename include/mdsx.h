@@ -276,7 +276,26 @@ typedef struct {
     double train_learning_rate;
     double fallback_accept;      /* 0.6 */
     int fallback_window;         /* e.g. 50 */
+    /* Checkpoint and resume of exact-gradient chains (no surrogate), so a long
+     * run can stop and continue: `checkpoint` (capacity checkpoint_capacity
+     * >= MDSX_HMC_CHECKPOINT_BYTES(N, P); NULL for none) receives the chain's
+     * state after its last iteration -- next iteration index, locations and
+     * their exact gradient, log-likelihood, log prior, potential, X'X, tau,
+     * trait precision, step size and step-size adaptation state, and the host
+     * random generator; stats->checkpoint_bytes gives its size. `resume`
+     * (NULL for a fresh chain) continues the chain such a checkpoint holds,
+     * with the same seed, engine dimensions and delta: initial_locations is
+     * ignored, `iterations` counts further iterations, burn_in stays counted
+     * from the chain's first iteration. A chain run in pieces this way gives
+     * the same trace, bit for bit, as the chain run in one call. */
+    const void* resume;
+    size_t resume_bytes;
+    void* checkpoint;
+    size_t checkpoint_capacity;
 } mdsx_hmc_config;
+
+#define MDSX_HMC_CHECKPOINT_BYTES(n, p) \
+    (112 + 16 * (size_t)(p) * (size_t)(p) + 16 * (size_t)(n) * (size_t)(p) + 8192)
 
 typedef struct {
     double accept_rate;              /* after burn-in */
@@ -288,6 +307,7 @@ typedef struct {
     int fallback_iteration;          /* iteration of the fallback to exact gradients, -1 if none */
     double train_seconds;            /* wall time of surrogate training */
     double train_loss;               /* mean loss over the last 10% of training steps */
+    long long checkpoint_bytes;      /* bytes written to config->checkpoint, 0 if none */
 } mdsx_hmc_stats;
 
 /* initial_locations: N*P host doubles; trace: iterations * (MDSX_HMC_TRACE_BASE +
@@ -374,6 +394,21 @@ int mdsx_batch_force_shape(mdsx_batch* batch, int p, int schedule, int rows_per_
 int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const double* d_locations,
                            int location_count, int embedding_dimension, double precision, int truncation,
                            double* d_sum_of_increments, double* d_gradient, void* stream);
+
+/* ---- Host-side fault injection (no counterpart in the reference, which
+ * asserts or exits on errors) ----
+ * For tests of the failure paths: arms one host-side call of `site` to fail
+ * after `after` further calls at that site succeed; the failing call is not
+ * made and the hook returns what the CUDA runtime would (out of memory, or a
+ * non-sticky launch failure), so no GPU fault occurs and the context stays
+ * usable. The engine and batch calls then return MDSX_ENOMEM or MDSX_ECUDA.
+ * One-shot: the hook disarms itself when it fires; MDSX_FAULT_NONE disarms.
+ * *fired (may be NULL) = faults fired so far in this process. */
+#define MDSX_FAULT_NONE 0
+#define MDSX_FAULT_DEVICE_ALLOC 1 /* cudaMalloc in engine and batch set-up */
+#define MDSX_FAULT_HOST_ALLOC 2   /* cudaMallocHost (pinned result mirrors) */
+#define MDSX_FAULT_LAUNCH 3       /* the enqueue of a sweep (engine) or of the batch graph */
+int mdsx_inject_fault(int site, long long after, long long* fired);
 
 /* Library version string. */
 const char* mdsx_version(void);

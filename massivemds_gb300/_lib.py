@@ -56,6 +56,7 @@ SIGNATURES = {
     "mdsx_hmc_run": (_i, [_vp, _vp, _dp, _dp, _dp, _vp]),
     "mdsx_sweep_f32_noalloc": (_i, [_vp, ctypes.c_longlong, _vp, _i, _i, ctypes.c_double, _i, _vp, _vp, _vp]),
     "mdsx_version": (ctypes.c_char_p, []),
+    "mdsx_inject_fault": (_i, [_i, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]),
     "mdsx_surrogate_create": (_i, [_vp, _i, _i, _i, _i, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
     "mdsx_surrogate_destroy": (None, [_vp]),
     "mdsx_surrogate_last_error": (ctypes.c_char_p, [_vp]),

@@ -41,6 +41,7 @@
 #include "normal_rational.h"
 #include "pair_plan.h"
 #include "sweep.h"
+#include "fault.h"
 
 namespace mdsx {
 namespace batch {
@@ -363,12 +364,12 @@ int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
         const int max_slots = q.max_slots;
         const int first_cta = q.first_cta;
         const int islots = q.ctas;
-        BCUDA(b, cudaMalloc(&in.d_prow, (size_t)q.units * mdsx::kPairRows * g.p * sizeof(float)));
-        BCUDA(b, cudaMalloc(&in.d_pcol,
+        BCUDA(b, mdsx::device_malloc(&in.d_prow, (size_t)q.units * mdsx::kPairRows * g.p * sizeof(float)));
+        BCUDA(b, mdsx::device_malloc(&in.d_pcol,
                             (size_t)q.nb * max_slots * mdsx::kPairWarps * g.p * mdsx::kPairCols * sizeof(float)));
-        BCUDA(b, cudaMalloc(&in.d_plp, (size_t)islots * mdsx::kPairWarps * 2 * sizeof(double)));
-        BCUDA(b, cudaMalloc(&in.d_pjfirst, (size_t)q.nb * sizeof(int)));
-        BCUDA(b, cudaMalloc(&in.d_pjslots, (size_t)q.nb * sizeof(int)));
+        BCUDA(b, mdsx::device_malloc(&in.d_plp, (size_t)islots * mdsx::kPairWarps * 2 * sizeof(double)));
+        BCUDA(b, mdsx::device_malloc(&in.d_pjfirst, (size_t)q.nb * sizeof(int)));
+        BCUDA(b, mdsx::device_malloc(&in.d_pjslots, (size_t)q.nb * sizeof(int)));
         BCUDA(b, cudaMemcpyAsync(in.d_pjfirst, jfirst.data(), (size_t)q.nb * sizeof(int), cudaMemcpyHostToDevice, st));
         BCUDA(b, cudaMemcpyAsync(in.d_pjslots, jslots.data(), (size_t)q.nb * sizeof(int), cudaMemcpyHostToDevice, st));
         BCUDA(b, cudaStreamSynchronize(st));  // the host tables go out of scope
@@ -403,8 +404,8 @@ int plan_pairs_group(mdsx_batch* b, BatchGroup& g) {
         g.h_pdesc.push_back(d);
     }
     g.finish_blocks = finish;
-    BCUDA(b, cudaMalloc(&g.d_pdesc, g.h_pdesc.size() * sizeof(mdsx::batch::PairInstance)));
-    BCUDA(b, cudaMalloc(&g.d_pbegin, (size_t)(G + 1) * sizeof(long long)));
+    BCUDA(b, mdsx::device_malloc(&g.d_pdesc, g.h_pdesc.size() * sizeof(mdsx::batch::PairInstance)));
+    BCUDA(b, mdsx::device_malloc(&g.d_pbegin, (size_t)(G + 1) * sizeof(long long)));
     BCUDA(b, cudaMemcpy(g.d_pbegin, begin.data(), (size_t)(G + 1) * sizeof(long long), cudaMemcpyHostToDevice));
     return MDSX_OK;
 }
@@ -484,7 +485,7 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
             BatchInst& in = b->inst[k];
             in.n_row_blocks = (in.n + rb - 1) / rb;
             in.rows_padded = in.n_row_blocks * rb;
-            BCUDA(b, cudaMalloc(&in.d_row_nan, (size_t)in.rows_padded * sizeof(int)));
+            BCUDA(b, mdsx::device_malloc(&in.d_row_nan, (size_t)in.rows_padded * sizeof(int)));
             BCUDA(b, mdsx::mark_nan_rows(in.d_delta, true, in.n, in.ld, in.d_row_nan, in.rows_padded, st));
             // flag row: 1 for rows with a NaN and for columns n .. x_ld (read by the pair schedule)
             BCUDA(b, mdsx::write_flag_row(in.d_row_nan, in.n, in.rows_padded, in.d_x + (size_t)g.p * in.x_ld, true,
@@ -518,11 +519,11 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
                                                         mdsx::cta_of_unit(u0, g.n_units, g.grid) + 1);
                 }
                 d.max_slots = max_slots;
-                BCUDA(b, cudaMalloc(&in.d_gpart, (size_t)d.n_row_blocks * max_slots * rb * g.p * sizeof(float)));
-                BCUDA(b, cudaMalloc(&in.d_lpart,
+                BCUDA(b, mdsx::device_malloc(&in.d_gpart, (size_t)d.n_row_blocks * max_slots * rb * g.p * sizeof(float)));
+                BCUDA(b, mdsx::device_malloc(&in.d_lpart,
                                     (size_t)d.n_row_blocks * max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
-                BCUDA(b, cudaMalloc(&in.d_lrow, (size_t)d.n_row_blocks * 2 * sizeof(double)));
-                BCUDA(b, cudaMalloc(&in.d_counts, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned)));
+                BCUDA(b, mdsx::device_malloc(&in.d_lrow, (size_t)d.n_row_blocks * 2 * sizeof(double)));
+                BCUDA(b, mdsx::device_malloc(&in.d_counts, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned)));
                 BCUDA(b, cudaMemsetAsync(in.d_counts, 0, ((size_t)d.n_row_blocks + 1) * sizeof(unsigned), st));
                 int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
                 if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p, in.x_ld, mdsx::kStepCols, g.p);
@@ -535,7 +536,7 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
                 d.rb_count = in.d_counts;
                 d.done_count = in.d_counts + d.n_row_blocks;
             }
-            BCUDA(b, cudaMalloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
+            BCUDA(b, mdsx::device_malloc(&g.d_desc, g.h_desc.size() * sizeof(BatchInstance)));
         } else if (g.schedule == 2) {
             // full residency, as the queue: the CTAs never wait on one another, so
             // concurrent groups simply share the SMs
@@ -556,8 +557,8 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
                 d.item_begin = g.n_items;
                 set_precision_constants(d, in.tau);
                 g.n_items += in.n_row_blocks;
-                BCUDA(b, cudaMalloc(&in.d_qlpart, (size_t)in.n_row_blocks * mdsx::kConsumerWarps * 2 * sizeof(double)));
-                BCUDA(b, cudaMalloc(&in.d_qdone, sizeof(unsigned)));
+                BCUDA(b, mdsx::device_malloc(&in.d_qlpart, (size_t)in.n_row_blocks * mdsx::kConsumerWarps * 2 * sizeof(double)));
+                BCUDA(b, mdsx::device_malloc(&in.d_qdone, sizeof(unsigned)));
                 BCUDA(b, cudaMemsetAsync(in.d_qdone, 0, sizeof(unsigned), st));
                 int rc = make_tmap(b, &d.tmap_delta, in.d_delta, in.n, in.n, in.ld, mdsx::kStepCols, rb);
                 if (!rc) rc = make_tmap(b, &d.tmap_x, in.d_x, in.n, g.p + 1, in.x_ld, mdsx::kStepCols, g.p + 1);
@@ -567,17 +568,17 @@ int plan(mdsx_batch* b, const std::map<std::pair<int, int>, Shape>* force = null
                 g.h_qdesc.push_back(d);
             }
             g.grid = (int)std::max<long long>(1, std::min<long long>(g.n_items, (long long)b->sm_count * g.ctas_per_sm));
-            BCUDA(b, cudaMalloc(&g.d_qdesc, g.h_qdesc.size() * sizeof(mdsx::batch::QueueInstance)));
-            BCUDA(b, cudaMalloc(&g.d_next, sizeof(unsigned long long)));
+            BCUDA(b, mdsx::device_malloc(&g.d_qdesc, g.h_qdesc.size() * sizeof(mdsx::batch::QueueInstance)));
+            BCUDA(b, mdsx::device_malloc(&g.d_next, sizeof(unsigned long long)));
         }
         b->groups.push_back(std::move(g));
     }
     b->grad_total = grad_off;
     const size_t count = b->inst.size();
-    BCUDA(b, cudaMalloc(&b->d_grad_all, (size_t)std::max<long long>(1, grad_off) * sizeof(double)));
-    BCUDA(b, cudaMalloc(&b->d_sums_all, count * 4 * sizeof(double)));
+    BCUDA(b, mdsx::device_malloc(&b->d_grad_all, (size_t)std::max<long long>(1, grad_off) * sizeof(double)));
+    BCUDA(b, mdsx::device_malloc(&b->d_sums_all, count * 4 * sizeof(double)));
     BCUDA(b, cudaMemsetAsync(b->d_sums_all, 0, count * 4 * sizeof(double), st));
-    BCUDA(b, cudaMallocHost(&b->h_results, (count * 4 + (size_t)grad_off) * sizeof(double)));
+    BCUDA(b, mdsx::host_malloc(&b->h_results, (count * 4 + (size_t)grad_off) * sizeof(double)));
     // output pointers (instance order in the sums array is the instance index)
     for (auto& g : b->groups) {
         for (size_t m = 0; m < g.h_desc.size(); ++m) {
@@ -733,6 +734,7 @@ int enqueue_evaluation(mdsx_batch* b) {
         BCUDA(b, cudaGraphInstantiate(&b->exec, gr, 0));
         b->graph_dirty = false;
     }
+    BCUDA(b, mdsx::launch_fault());
     BCUDA(b, cudaGraphLaunch(b->exec, b->stream));
     ++b->evaluations;
     return MDSX_OK;
@@ -790,7 +792,7 @@ int mdsx_batch_create(long flags, int device, mdsx_batch** out) {
     if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming) != cudaSuccess ||
-        cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess || cudaMemset(b->d_err, 0, sizeof(int)) != cudaSuccess) {
+        mdsx::device_malloc(&b->d_err, sizeof(int)) != cudaSuccess || cudaMemset(b->d_err, 0, sizeof(int)) != cudaSuccess) {
         if (b->stream) cudaStreamDestroy(b->stream);
         if (b->uploaded) cudaEventDestroy(b->uploaded);
         cudaFree(b->d_err);
@@ -838,10 +840,10 @@ int mdsx_batch_add_instance(mdsx_batch* b, int embedding_dimension, int location
     in.ld = mdsx::batch::round_up(in.n, 4);
     in.x_ld = (int)mdsx::batch::round_up(in.n, mdsx::kStepCols);
     const size_t xb = (size_t)(in.p + 1) * in.x_ld * sizeof(float);  // row P: missing-row flags
-    if (cudaMalloc(&in.d_delta, (size_t)in.n * in.ld * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&in.d_x, xb) != cudaSuccess ||
-        cudaMalloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost(&in.h_x, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
+    if (mdsx::device_malloc(&in.d_delta, (size_t)in.n * in.ld * sizeof(float)) != cudaSuccess ||
+        mdsx::device_malloc(&in.d_x, xb) != cudaSuccess ||
+        mdsx::device_malloc(&in.d_xin, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess ||
+        mdsx::host_malloc(&in.h_x, (size_t)in.n * in.p * sizeof(double)) != cudaSuccess) {
         cudaFree(in.d_delta);
         cudaFree(in.d_x);
         cudaFree(in.d_xin);

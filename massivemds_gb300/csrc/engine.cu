@@ -31,6 +31,7 @@
 #include "pair_plan.h"
 #include "engine_internal.h"
 #include "sweep.h"
+#include "fault.h"
 
 
 
@@ -131,18 +132,18 @@ int plan_pairs(mdsx_engine* e) {
     const std::vector<long long>& begin = plan.cta_begin;
     const std::vector<int>& jfirst = q.j_first;
     const std::vector<int>& jslots = q.j_slots;
-    MDSX_CUDA(e, cudaMalloc(&e->d_pair_begin, (size_t)(G + 1) * sizeof(long long)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_pair_jfirst, (size_t)e->pair_nb * sizeof(int)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_pair_jslots, (size_t)e->pair_nb * sizeof(int)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_pair_begin, (size_t)(G + 1) * sizeof(long long)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_pair_jfirst, (size_t)e->pair_nb * sizeof(int)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_pair_jslots, (size_t)e->pair_nb * sizeof(int)));
     MDSX_CUDA(e, cudaMemcpy(e->d_pair_begin, begin.data(), (size_t)(G + 1) * sizeof(long long),
                             cudaMemcpyHostToDevice));
     MDSX_CUDA(e, cudaMemcpy(e->d_pair_jfirst, jfirst.data(), (size_t)e->pair_nb * sizeof(int), cudaMemcpyHostToDevice));
     MDSX_CUDA(e, cudaMemcpy(e->d_pair_jslots, jslots.data(), (size_t)e->pair_nb * sizeof(int), cudaMemcpyHostToDevice));
     const size_t part_bytes = f64 ? sizeof(double) : sizeof(float);
-    MDSX_CUDA(e, cudaMalloc(&e->d_rowpart, (size_t)e->pair_units * mdsx::kPairRows * e->p * part_bytes));
-    MDSX_CUDA(e, cudaMalloc(&e->d_colpart, (size_t)e->pair_nb * e->pair_max_slots * mdsx::kPairWarps * e->p *
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_rowpart, (size_t)e->pair_units * mdsx::kPairRows * e->p * part_bytes));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_colpart, (size_t)e->pair_nb * e->pair_max_slots * mdsx::kPairWarps * e->p *
                                                mdsx::kPairCols * part_bytes));
-    MDSX_CUDA(e, cudaMalloc(&e->d_plpart, (size_t)e->pair_grid * mdsx::kPairWarps * 2 * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_plpart, (size_t)e->pair_grid * mdsx::kPairWarps * 2 * sizeof(double)));
     for (int b = 0; b < 2; ++b) {
         mdsx::PairMaps& m = e->pair_maps[b];
         int rc = make_tmap_2d(e, &m.a, e->d_delta, e->delta_f32, e->n, e->n, e->ld, mdsx::kPairCols,
@@ -189,25 +190,25 @@ int plan_and_allocate(mdsx_engine* e) {
     const size_t x_bytes = (size_t)(e->p + 1) * e->x_ld * e->shape.x_elem_bytes;
     const size_t acc_bytes = e->x_f32 ? 4 : 8;
 
-    MDSX_CUDA(e, cudaMalloc(&e->d_delta, (size_t)e->rows * e->ld * delta_elem));
-    MDSX_CUDA(e, cudaMalloc(&e->d_x[0], x_bytes));
-    MDSX_CUDA(e, cudaMalloc(&e->d_x[1], x_bytes));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_delta, (size_t)e->rows * e->ld * delta_elem));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_x[0], x_bytes));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_x[1], x_bytes));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_x[0], 0, x_bytes, e->stream));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_x[1], 0, x_bytes, e->stream));
-    MDSX_CUDA(e, cudaMalloc(&e->d_xin, (size_t)e->n * e->p * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_grad[0], (size_t)e->rows * e->p * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_grad[1], (size_t)e->rows * e->p * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_out, 4 * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_xin, (size_t)e->n * e->p * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_grad[0], (size_t)e->rows * e->p * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_grad[1], (size_t)e->rows * e->p * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_out, 4 * sizeof(double)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_out, 0, 4 * sizeof(double), e->stream));
-    MDSX_CUDA(e, cudaMalloc(&e->d_gpart, (size_t)e->n_row_blocks * e->max_slots * rb * e->p * acc_bytes));
-    MDSX_CUDA(e, cudaMalloc(&e->d_lpart,
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_gpart, (size_t)e->n_row_blocks * e->max_slots * rb * e->p * acc_bytes));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_lpart,
                             (size_t)e->n_row_blocks * e->max_slots * mdsx::kConsumerWarps * 2 * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_lrow, (size_t)e->n_row_blocks * 2 * sizeof(double)));
-    MDSX_CUDA(e, cudaMalloc(&e->d_counts, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_lrow, (size_t)e->n_row_blocks * 2 * sizeof(double)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_counts, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_counts, 0, ((size_t)e->n_row_blocks + 1) * sizeof(unsigned), e->stream));
-    MDSX_CUDA(e, cudaMalloc(&e->d_row_nan, (size_t)e->rows_padded * sizeof(int)));
+    MDSX_CUDA(e, mdsx::device_malloc(&e->d_row_nan, (size_t)e->rows_padded * sizeof(int)));
     MDSX_CUDA(e, cudaMemsetAsync(e->d_row_nan, 0, (size_t)e->rows_padded * sizeof(int), e->stream));
-    MDSX_CUDA(e, cudaMallocHost(&e->h_out, 4 * sizeof(double)));
+    MDSX_CUDA(e, mdsx::host_malloc(&e->h_out, 4 * sizeof(double)));
 
     int rc = make_tmap_2d(e, &e->tmap_delta, e->d_delta, e->delta_f32, e->n, e->rows, e->ld, mdsx::kStepCols, rb);
     if (rc) return rc;
@@ -327,6 +328,7 @@ mdsx::PairArgs make_pair_args(mdsx_engine* e) {
 int enqueue_sweep(mdsx_engine* e) {
     if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
     if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
+    MDSX_CUDA(e, mdsx::launch_fault());
     if (e->schedule == MDSX_SWEEP_PAIRS) {
         const mdsx::PairArgs pa = make_pair_args(e);
         MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
@@ -347,6 +349,7 @@ int enqueue_sweep_leapfrog(mdsx_engine* e, const mdsx::PairLeapfrog& lf) {
     if (!e->data_set) return fail(e, MDSX_ESTATE, "setPairwiseData has not been called");
     if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "precision (setParameters) not set");
     if (e->schedule != MDSX_SWEEP_PAIRS) return MDSX_EUNSUPPORTED;
+    MDSX_CUDA(e, mdsx::launch_fault());
     mdsx::PairArgs pa = make_pair_args(e);
     pa.leapfrog = 1;
     pa.leap = lf;
@@ -571,7 +574,7 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
         const long long chunk_elems = 16LL << 20;  // 128 MB of doubles
         const long long rows_per_chunk = std::max(1LL, chunk_elems / e->n);
         double* staging = nullptr;
-        MDSX_CUDA(e, cudaMalloc(&staging, (size_t)std::min<long long>(rows_per_chunk, e->rows) * e->n * sizeof(double)));
+        MDSX_CUDA(e, mdsx::device_malloc(&staging, (size_t)std::min<long long>(rows_per_chunk, e->rows) * e->n * sizeof(double)));
         const int elem = e->delta_f32 ? 4 : 8;
         for (long long r0 = 0; r0 < e->rows; r0 += rows_per_chunk) {
             const long long rows = std::min<long long>(rows_per_chunk, e->rows - r0);

@@ -42,6 +42,7 @@
 #include <cmath>
 #include <cstring>
 #include <random>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -612,13 +613,80 @@ struct Chain {
 
 using mdsx::hmc::Chain;
 
+namespace mdsx {
+namespace hmc {
+namespace {
+
+// Chain checkpoint: a fixed header, then s0 (P*P), Lambda (P*P), x0 (N*P),
+// gl0 (N*P) and the host generator's state as text (std::mt19937_64 << ).
+constexpr char kCkptMagic[8] = {'M', 'D', 'S', 'X', 'H', 'M', 'C', '2'};
+struct CkptHeader {
+    char magic[8];
+    int32_t n, p;
+    uint64_t seed;
+    int64_t next_iteration;
+    double tau, eps, hbar, log_eps_bar, loglik0, logprior0, u0;
+    int32_t rng_len, pad;
+    int64_t reserved[2];
+};
+static_assert(sizeof(CkptHeader) == 112, "checkpoint header layout");
+
+struct CkptState {
+    CkptHeader h{};
+    std::vector<double> s0, lambda, x0, gl0;
+    std::string rng;
+};
+
+size_t ckpt_bytes(const CkptState& c) {
+    return sizeof(CkptHeader) + 8 * (c.s0.size() + c.lambda.size() + c.x0.size() + c.gl0.size()) + c.rng.size();
+}
+
+bool ckpt_read(const void* src, size_t bytes, int n, int p, CkptState* out) {
+    if (!src || bytes < sizeof(CkptHeader)) return false;
+    const unsigned char* b = static_cast<const unsigned char*>(src);
+    std::memcpy(&out->h, b, sizeof(CkptHeader));
+    if (std::memcmp(out->h.magic, kCkptMagic, 8) != 0 || out->h.n != n || out->h.p != p || out->h.rng_len < 0 ||
+        out->h.rng_len > 8192)
+        return false;
+    const size_t pp = (size_t)p * p, np = (size_t)n * p;
+    if (bytes != sizeof(CkptHeader) + 8 * (2 * pp + 2 * np) + (size_t)out->h.rng_len) return false;
+    size_t off = sizeof(CkptHeader);
+    auto take = [&](std::vector<double>& v, size_t count) {
+        v.resize(count);
+        std::memcpy(v.data(), b + off, 8 * count);
+        off += 8 * count;
+    };
+    take(out->s0, pp);
+    take(out->lambda, pp);
+    take(out->x0, np);
+    take(out->gl0, np);
+    out->rng.assign(reinterpret_cast<const char*>(b + off), (size_t)out->h.rng_len);
+    return true;
+}
+
+void ckpt_write(const CkptState& c, void* dst) {
+    unsigned char* b = static_cast<unsigned char*>(dst);
+    std::memcpy(b, &c.h, sizeof(CkptHeader));
+    size_t off = sizeof(CkptHeader);
+    for (const std::vector<double>* v : {&c.s0, &c.lambda, &c.x0, &c.gl0}) {
+        std::memcpy(b + off, v->data(), 8 * v->size());
+        off += 8 * v->size();
+    }
+    std::memcpy(b + off, c.rng.data(), c.rng.size());
+}
+
+}  // namespace
+}  // namespace hmc
+}  // namespace mdsx
+
 extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const double* initial_locations,
                             double* trace, double* final_locations, mdsx_hmc_stats* stats) {
     using namespace mdsx::hmc;
     using mdsx::internal::fail;
     if (!e) return MDSX_EINVAL;
     if (!cfg || !initial_locations || !trace) return fail(e, MDSX_EINVAL, "hmc: NULL argument");
-    if (cfg->iterations < 1 || cfg->burn_in < 0 || cfg->burn_in > cfg->iterations || cfg->leapfrog_steps < 1 ||
+    if (cfg->iterations < 1 || cfg->burn_in < 0 || (!cfg->resume && !cfg->checkpoint && cfg->burn_in > cfg->iterations) ||
+        cfg->leapfrog_steps < 1 ||
         !(cfg->step_size > 0.0) || cfg->n_traced_pairs < 0 || cfg->n_traced_locations < 0)
         return fail(e, MDSX_EINVAL, "hmc: bad configuration");
     if ((cfg->n_traced_pairs && !cfg->traced_pairs) || (cfg->n_traced_locations && !cfg->traced_locations))
@@ -635,6 +703,18 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         return fail(e, MDSX_EINVAL, "hmc: precision_half_width must be > 0");
     if (cfg->adapt_step_size && !(cfg->target_accept > 0.0 && cfg->target_accept < 1.0))
         return fail(e, MDSX_EINVAL, "hmc: target_accept must be in (0, 1)");
+    if (cfg->surrogate && (cfg->resume || cfg->checkpoint))
+        return fail(e, MDSX_EUNSUPPORTED, "hmc: checkpoint and resume are for exact-gradient chains");
+    if (cfg->checkpoint && cfg->checkpoint_capacity < MDSX_HMC_CHECKPOINT_BYTES(e->n, e->p))
+        return fail(e, MDSX_EINVAL, "hmc: checkpoint capacity below MDSX_HMC_CHECKPOINT_BYTES(N, P)");
+    CkptState resume_state;
+    if (cfg->resume) {
+        if (!ckpt_read(cfg->resume, cfg->resume_bytes, e->n, e->p, &resume_state))
+            return fail(e, MDSX_EINVAL, "hmc: resume data is not a checkpoint of a chain with these dimensions");
+        if (resume_state.h.seed != cfg->seed) return fail(e, MDSX_EINVAL, "hmc: resume with the chain's own seed");
+        if (!(resume_state.h.tau > 0.0) || !(resume_state.h.eps > 0.0))
+            return fail(e, MDSX_EINVAL, "hmc: checkpoint holds a bad precision or step size");
+    }
     if (cfg->surrogate) {
         if (cfg->surrogate->engine != e) return fail(e, MDSX_EINVAL, "hmc: the surrogate belongs to another engine");
         if (cfg->harvest_iterations < 0 || cfg->harvest_iterations > cfg->iterations || cfg->harvest_rows < 0 ||
@@ -655,39 +735,67 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
     c.s = e->stream;
     c.rng.seed(cfg->seed ^ 0x5DEECE66DULL);
     c.eps = cfg->step_size;
+    const long long it0 = cfg->resume ? resume_state.h.next_iteration : 0;
+    if (cfg->resume) {
+        std::istringstream in(resume_state.rng);
+        in >> c.rng;
+        if (in.fail()) return fail(e, MDSX_EINVAL, "hmc: checkpoint holds a bad generator state");
+        c.eps = resume_state.h.eps;
+        e->tau = resume_state.h.tau;
+        e->sum_known = e->grad_known = false;
+    }
     int rc = c.alloc();
     if (rc) return rc;
     const int n = c.n, p = c.p;
     const int cols = kTraceBase + c.n_func;
 
-    // Lambda = I_P (R/Untitled.R:537-540 without a tree: traitVcv = diag(P)).
-    {
+    // Lambda = I_P (R/Untitled.R:537-540 without a tree: traitVcv = diag(P)), or the checkpoint's.
+    if (cfg->resume) {
+        if ((rc = c.set_lambda(resume_state.lambda.data()))) return rc;
+    } else {
         double eye[kMaxP * kMaxP] = {};
         for (int q = 0; q < p; ++q) eye[q * p + q] = 1.0;
         if ((rc = c.set_lambda(eye))) return rc;
     }
     if ((rc = c.set_coef())) return rc;
 
-    // Initial state: x0, its likelihood gradient, potential and X'X.
-    MDSX_CUDA(e, cudaMemcpyAsync(c.x0, initial_locations, (size_t)n * p * sizeof(double), cudaMemcpyHostToDevice, c.s));
-    MDSX_CUDA(e, mdsx::convert_locations(c.x0, n, p, e->d_x[e->xcur], e->x_ld, e->x_f32, c.s));
-    double loglik0 = 0.0;
-    if ((rc = c.sweep_loglik(&loglik0))) return rc;
-    MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, e->d_grad[e->gcur], (size_t)n * p * sizeof(double), cudaMemcpyDeviceToDevice, c.s));
-    if ((rc = c.reduce(1, c.x0, c.red_q))) return rc;
-    MDSX_CUDA(e, cudaMemcpyAsync(c.h_q(), c.red_q, (p * p + 1) * sizeof(double), cudaMemcpyDeviceToHost, c.s));
-    MDSX_CUDA(e, cudaStreamSynchronize(c.s));
-    std::vector<double> s0(c.h_q(), c.h_q() + p * p);
-    double logprior0 = c.log_prior(c.h_q()[p * p]);
-    double u0 = -(loglik0 + logprior0);
+    // Initial state: x0, its likelihood gradient, potential and X'X (from the
+    // checkpoint when resuming, so the continued chain is the same chain).
+    double loglik0 = 0.0, logprior0 = 0.0, u0 = 0.0;
+    std::vector<double> s0;
+    if (cfg->resume) {
+        MDSX_CUDA(e, cudaMemcpyAsync(c.x0, resume_state.x0.data(), (size_t)n * p * sizeof(double),
+                                     cudaMemcpyHostToDevice, c.s));
+        MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, resume_state.gl0.data(), (size_t)n * p * sizeof(double),
+                                     cudaMemcpyHostToDevice, c.s));
+        MDSX_CUDA(e, mdsx::convert_locations(c.x0, n, p, e->d_x[e->xcur], e->x_ld, e->x_f32, c.s));
+        MDSX_CUDA(e, cudaStreamSynchronize(c.s));
+        loglik0 = resume_state.h.loglik0;
+        logprior0 = resume_state.h.logprior0;
+        u0 = resume_state.h.u0;
+        s0 = resume_state.s0;
+    } else {
+        MDSX_CUDA(e, cudaMemcpyAsync(c.x0, initial_locations, (size_t)n * p * sizeof(double), cudaMemcpyHostToDevice,
+                                     c.s));
+        MDSX_CUDA(e, mdsx::convert_locations(c.x0, n, p, e->d_x[e->xcur], e->x_ld, e->x_f32, c.s));
+        if ((rc = c.sweep_loglik(&loglik0))) return rc;
+        MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, e->d_grad[e->gcur], (size_t)n * p * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, c.s));
+        if ((rc = c.reduce(1, c.x0, c.red_q))) return rc;
+        MDSX_CUDA(e, cudaMemcpyAsync(c.h_q(), c.red_q, (p * p + 1) * sizeof(double), cudaMemcpyDeviceToHost, c.s));
+        MDSX_CUDA(e, cudaStreamSynchronize(c.s));
+        s0.assign(c.h_q(), c.h_q() + p * p);
+        logprior0 = c.log_prior(c.h_q()[p * p]);
+        u0 = -(loglik0 + logprior0);
+    }
 
     // dual averaging (Hoffman & Gelman 2014, Algorithm 5)
     const double mu = std::log(10.0 * cfg->step_size), gamma = 0.05, t0 = 10.0, kappa = 0.75;
-    double hbar = 0.0, log_eps_bar = 0.0;
+    double hbar = cfg->resume ? resume_state.h.hbar : 0.0, log_eps_bar = cfg->resume ? resume_state.h.log_eps_bar : 0.0;
     std::uniform_real_distribution<double> unif(0.0, 1.0);
-    long long accepted_after = 0;
+    long long accepted_after = 0, kept = 0;
     auto t_start = std::chrono::steady_clock::now();
-    bool timing = cfg->burn_in == 0;
+    bool timing = it0 >= cfg->burn_in;
     // surrogate phase
     mdsx_surrogate* const sg = cfg->surrogate;
     bool surr_ready = false;
@@ -721,7 +829,8 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
     };
     if (sg && cfg->harvest_iterations == 0 && (rc = start_surrogate())) return rc;
 
-    for (int it = 0; it < cfg->iterations; ++it) {
+    for (int k_it = 0; k_it < cfg->iterations; ++k_it) {
+        const int it = (int)(it0 + k_it);  // the chain's iteration index (keys the momentum draws)
         if (!timing && it == cfg->burn_in) {
             timing = true;
             t_start = std::chrono::steady_clock::now();
@@ -764,7 +873,10 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
             u0 = u_p;
             s0.assign(c.h_q(), c.h_q() + p * p);
         }
-        if (it >= cfg->burn_in && accept) ++accepted_after;
+        if (it >= cfg->burn_in) {
+            ++kept;
+            if (accept) ++accepted_after;
+        }
         // harvest (chain state, its exact gradient)
         if (sg && it >= cfg->harvest_start && it < cfg->harvest_iterations && cfg->harvest_rows > 0) {
             rc = mdsx::surr::add_state(sg, c.x0, c.gl0, cfg->harvest_rows,
@@ -841,7 +953,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         if (sg && !surr_ready && it + 1 == cfg->harvest_iterations && (rc = start_surrogate())) return rc;
 
         // trace row
-        double* row = trace + (size_t)it * cols;
+        double* row = trace + (size_t)k_it * cols;
         row[0] = loglik0;
         row[1] = logprior0;
         row[2] = u0;
@@ -869,8 +981,40 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
     MDSX_CUDA(e, cudaStreamSynchronize(c.s));
     e->sum_known = false;
     e->grad_known = false;
+    long long ckpt_size = 0;
+    if (cfg->checkpoint) {
+        CkptState out;
+        std::memcpy(out.h.magic, kCkptMagic, 8);
+        out.h.n = n;
+        out.h.p = p;
+        out.h.seed = cfg->seed;
+        out.h.next_iteration = it0 + cfg->iterations;
+        out.h.tau = e->tau;
+        out.h.eps = c.eps;
+        out.h.hbar = hbar;
+        out.h.log_eps_bar = log_eps_bar;
+        out.h.loglik0 = loglik0;
+        out.h.logprior0 = logprior0;
+        out.h.u0 = u0;
+        out.s0 = s0;
+        out.lambda.assign(c.lam.m, c.lam.m + p * p);
+        out.x0.resize((size_t)n * p);
+        out.gl0.resize((size_t)n * p);
+        MDSX_CUDA(e, cudaMemcpyAsync(out.x0.data(), c.x0, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToHost, c.s));
+        MDSX_CUDA(e, cudaMemcpyAsync(out.gl0.data(), c.gl0, (size_t)n * p * sizeof(double), cudaMemcpyDeviceToHost,
+                                     c.s));
+        MDSX_CUDA(e, cudaStreamSynchronize(c.s));
+        std::ostringstream os;
+        os << c.rng;
+        out.rng = os.str();
+        out.h.rng_len = (int32_t)out.rng.size();
+        if (out.rng.size() > 8192 || ckpt_bytes(out) > cfg->checkpoint_capacity)
+            return fail(e, MDSX_EINVAL, "hmc: checkpoint larger than its buffer");
+        ckpt_write(out, cfg->checkpoint);
+        ckpt_size = (long long)ckpt_bytes(out);
+    }
     if (stats) {
-        const int kept = cfg->iterations - cfg->burn_in;
+        stats->checkpoint_bytes = ckpt_size;
         stats->accept_rate = kept > 0 ? (double)accepted_after / kept : 0.0;
         stats->step_size = c.eps;
         stats->seconds = seconds;

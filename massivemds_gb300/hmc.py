@@ -47,6 +47,10 @@ class _Config(ctypes.Structure):
         ("train_learning_rate", ctypes.c_double),
         ("fallback_accept", ctypes.c_double),
         ("fallback_window", ctypes.c_int),
+        ("resume", ctypes.c_void_p),
+        ("resume_bytes", ctypes.c_size_t),
+        ("checkpoint", ctypes.c_void_p),
+        ("checkpoint_capacity", ctypes.c_size_t),
     ]
 
 
@@ -61,6 +65,7 @@ class _Stats(ctypes.Structure):
         ("fallback_iteration", ctypes.c_int),
         ("train_seconds", ctypes.c_double),
         ("train_loss", ctypes.c_double),
+        ("checkpoint_bytes", ctypes.c_longlong),
     ]
 
 
@@ -79,6 +84,7 @@ class HmcResult:
     fallback_iteration: int = -1
     train_seconds: float = 0.0
     train_loss: float = float("nan")
+    checkpoint: bytes | None = None  # the chain's state after its last iteration (``checkpoint=True``)
 
     def column(self, name: str) -> np.ndarray:
         return self.trace[:, TRACE_COLUMNS.index(name)]
@@ -97,7 +103,8 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
         learn_precision: bool = False, precision_half_width: float = 0.01, learn_trait_precision: bool = False,
         seed: int = 666, traced_pairs=None, traced_locations=None, use_graph: bool = True, surrogate=None,
         harvest_iterations: int = 0, harvest_start: int | None = None, harvest_rows: int = 100, train_steps: int = 2000, train_batch: int = 512,
-        train_learning_rate: float = 1e-3, fallback_accept: float = 0.6, fallback_window: int = 50) -> HmcResult:
+        train_learning_rate: float = 1e-3, fallback_accept: float = 0.6, fallback_window: int = 50,
+        checkpoint: bool = False, resume: bytes | None = None) -> HmcResult:
     """Runs one chain on the engine's GPU; the engine must hold delta and tau.
 
     Defaults follow the reference: 20 leapfrog steps of 0.01 (trajectory 0.2,
@@ -110,6 +117,12 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
     with the exact potential deciding every accept, until the acceptance over
     the last ``fallback_window`` surrogate iterations drops below
     ``fallback_accept`` (exact gradients from then on).
+
+    ``checkpoint=True`` returns the chain's state after its last iteration in
+    ``HmcResult.checkpoint``; ``resume=<those bytes>`` (same engine, delta and
+    seed) continues that chain for ``iterations`` more iterations, ignoring
+    ``initial_locations``, with ``burn_in`` still counted from the chain's
+    first iteration. Exact-gradient chains only. See :func:`save_checkpoint`.
     """
     lib = load()
     n, p = engine.locationCount, engine.embeddingDimension
@@ -125,6 +138,13 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
                   int(harvest_iterations), int(harvest_iterations // 2 if harvest_start is None else harvest_start),
                   int(harvest_rows), int(train_steps), int(train_batch),
                   float(train_learning_rate), float(fallback_accept), int(fallback_window))
+    resume_buf = ctypes.create_string_buffer(bytes(resume), len(resume)) if resume is not None else None
+    cap = lib_checkpoint_bytes(n, p) if checkpoint else 0
+    ckpt_buf = ctypes.create_string_buffer(cap) if checkpoint else None
+    cfg.resume = ctypes.cast(resume_buf, ctypes.c_void_p) if resume_buf is not None else None
+    cfg.resume_bytes = len(resume) if resume is not None else 0
+    cfg.checkpoint = ctypes.cast(ckpt_buf, ctypes.c_void_p) if ckpt_buf is not None else None
+    cfg.checkpoint_capacity = cap
     cols = TRACE_BASE + len(pairs) + len(locs)
     trace = np.empty((iterations, cols), dtype=np.float64)
     final = np.empty((n, p), dtype=np.float64)
@@ -133,6 +153,29 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
     check(lib.mdsx_hmc_run(engine._h, ctypes.c_void_p(ctypes.addressof(cfg)), x0.ctypes.data_as(dp),
                            trace.ctypes.data_as(dp), final.ctypes.data_as(dp),
                            ctypes.c_void_p(ctypes.addressof(stats))), engine._h)
+    ckpt = ckpt_buf.raw[:stats.checkpoint_bytes] if checkpoint else None
     return HmcResult(trace, final, stats.accept_rate, stats.step_size, stats.seconds, stats.gradient_evaluations,
                      stats.precision, len(pairs), len(locs), stats.surrogate_evaluations, stats.fallback_iteration,
-                     stats.train_seconds, stats.train_loss)
+                     stats.train_seconds, stats.train_loss, ckpt)
+
+
+def lib_checkpoint_bytes(n: int, p: int) -> int:
+    """MDSX_HMC_CHECKPOINT_BYTES(N, P): the buffer a chain checkpoint needs."""
+    return 112 + 16 * p * p + 16 * n * p + 8192
+
+
+def save_checkpoint(path: str, data: bytes) -> None:
+    """Writes a chain checkpoint to a file (atomically: a temporary file, then a rename)."""
+    import os
+
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(data)
+        f.flush()
+        os.fsync(f.fileno())
+    os.replace(tmp, path)
+
+
+def load_checkpoint(path: str) -> bytes:
+    with open(path, "rb") as f:
+        return f.read()

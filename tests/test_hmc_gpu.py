@@ -114,3 +114,50 @@ def test_precision_and_trait_precision_moves():
     s = e.getSumOfIncrements()
     e.close()
     assert abs(s - oracle.sum_of_increments(delta.astype(np.float32), res.final_locations, tau_final)) < 1e-5 * abs(s)
+
+
+@pytest.mark.parametrize("flags", [0, F.FLOAT])
+def test_checkpoint_and_resume_continue_the_same_chain(flags, tmp_path):
+    """A chain run in two calls -- the first writing a checkpoint, the second
+    resuming from it (through a file) -- gives the trace of the chain run in
+    one call, bit for bit: momentum keyed by the chain's iteration index, the
+    host generator, tau, the trait precision and the step-size adaptation
+    (its burn-in spans the split) all carry over."""
+    from massivemds_gb300.hmc import load_checkpoint, save_checkpoint
+
+    n, p, tau = 120, 2, 1.1
+    delta, x0 = _problem(n, p, 8, clusters=3)
+    kw = dict(leapfrog_steps=6, step_size=0.004, adapt_step_size=True, target_accept=0.8, burn_in=30,
+              learn_precision=True, precision_half_width=0.05, learn_trait_precision=True, seed=99,
+              traced_pairs=[[0, 1], [5, 77]], traced_locations=[3, 60])
+    e = _engine(delta, p, tau, flags)
+    whole = hmc(e, x0, iterations=50, **kw)
+    e.setParameters([tau])
+    first = hmc(e, x0, iterations=20, checkpoint=True, **kw)
+    assert first.checkpoint is not None and len(first.checkpoint) > 16 * n * p
+    path = str(tmp_path / "chain.ckpt")
+    save_checkpoint(path, first.checkpoint)
+    e.setParameters([3.0])  # resuming restores the chain's own precision
+    rest = hmc(e, np.zeros_like(x0), iterations=30, resume=load_checkpoint(path), **kw)  # locations come from the checkpoint
+    e.close()
+    assert np.array_equal(np.vstack([first.trace, rest.trace]), whole.trace)
+    assert np.array_equal(rest.final_locations, whole.final_locations)
+    assert rest.precision == whole.precision and rest.step_size == whole.step_size
+
+
+def test_resume_rejects_a_foreign_checkpoint():
+    from massivemds_gb300 import MdsxError
+
+    n, p = 60, 2
+    delta, x0 = _problem(n, p, 9)
+    e = _engine(delta, p, 1.0, 0)
+    first = hmc(e, x0, iterations=3, step_size=0.003, seed=1, checkpoint=True)
+    with pytest.raises(MdsxError):
+        hmc(e, x0, iterations=3, step_size=0.003, seed=2, resume=first.checkpoint)  # another seed
+    with pytest.raises(MdsxError):
+        hmc(e, x0, iterations=3, step_size=0.003, seed=1, resume=first.checkpoint[:-5])  # truncated
+    e.close()
+    e3 = _engine(_problem(n, 3, 9)[0], 3, 1.0, 0)
+    with pytest.raises(MdsxError):
+        hmc(e3, np.zeros((n, 3)), iterations=3, step_size=0.003, seed=1, resume=first.checkpoint)  # P differs
+    e3.close()
