@@ -59,6 +59,15 @@ constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
 constexpr int kPairMaxP = 6;     // FP32 pair math: P <= 4 row packs (PairMathF32), 5..6 column packs
 constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_ctas_of)
+#ifndef MDSX_PAIR_F32_STAGES
+#define MDSX_PAIR_F32_STAGES 3  // TMA ring depth of the FP32 pair kernels
+#endif
+#ifndef MDSX_PAIR_F32_CTAS
+#define MDSX_PAIR_F32_CTAS 2  // CTAs per SM of the FP32 pair kernels with P = 1, 2, 3, 5
+#endif
+#ifndef MDSX_PAIR_EARLY_RELEASE
+#define MDSX_PAIR_EARLY_RELEASE 1  // FP32 packs of rows: operands to registers, stage released before the math
+#endif
 
 // XB: bytes per location element (4: FP32 math, 8: FP64 math); SB: bytes per
 // delta element. FP64 math is bound by the FP64 pipe, so two stages hide the
@@ -66,7 +75,7 @@ constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_cta
 // come as two 128-byte-swizzled boxes of 16 columns (kBBoxes), one after the other.
 template <int P, int XB, int SB = 4>
 struct PairShape {
-    static constexpr int kStages = XB == 4 ? 3 : 2;
+    static constexpr int kStages = XB == 4 ? MDSX_PAIR_F32_STAGES : 2;
     static constexpr int kBBoxCols = 128 / SB;
     static constexpr int kBBoxes = kPairRows / kBBoxCols;
     static constexpr int kBBytes = kPairCols * kPairRows * SB;
@@ -212,23 +221,56 @@ __device__ __forceinline__ void pair_pack(const f2 (&xi)[P], const f2 (&nxj)[P],
     }
 }
 
-// One unit for one consumer warp: 4 rows x 4 columns per lane, both directions.
-// sA: the unit's A box; sBl: this lane's 16-byte chunk of B row `lane`
-// (swizzled); i0 = first row of the warp, j0 = first column of the block.
+// One consumer warp's operands of one unit, held in registers so the warp can
+// release the unit's stage before the pair math: the A packs (rows 4w + 2rp,
+// 4w + 2rp + 1 of column lane + 32c), this lane's 16-byte chunks of B rows
+// lane + 32c (rows 4w .. 4w+3 of the chunk) and the (x_i, x_i+1) packs.
+template <int P>
+struct PairOperandsF32 {
+    f2 a[4][2];
+    float4 b[4];
+    f2 xi[2][P];
+};
+
+template <int P>
+__device__ __forceinline__ void pair_load_f32(PairOperandsF32<P>& o, const float* __restrict__ sA,
+                                              const float* __restrict__ sB, const float* __restrict__ sXI, int lane,
+                                              int warp) {
+    // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
+    // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
+    const float* sBl = sB + lane * kPairRows + ((warp ^ (lane & 7)) << 2);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        o.b[c] = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+#pragma unroll
+        for (int rp = 0; rp < 2; ++rp)
+            o.a[c][rp] = pk(sA[(4 * warp + 2 * rp) * kPairCols + lane + 32 * c],
+                            sA[(4 * warp + 2 * rp + 1) * kPairCols + lane + 32 * c]);
+    }
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        const float4 x4 = *reinterpret_cast<const float4*>(sXI + q * kPairRows + 4 * warp);
+        o.xi[0][q] = pk(x4.x, x4.y);
+        o.xi[1][q] = pk(x4.z, x4.w);
+    }
+}
+
+// One unit for one consumer warp: 4 rows x 4 columns per lane, both directions,
+// from the operands in registers; i0 = first row of the warp, j0 = first column
+// of the block.
 template <int P, bool TRUNC, bool MASKED>
-__device__ __forceinline__ void pair_unit(const float* __restrict__ sA, const float* __restrict__ sBl,
-                                          const f2 (&xi)[2][P], const f2 (&nxj)[4][P], int i0, int j0, int n,
-                                          int lane, int wr, const PairConstsF32& k, f2 (&racc)[2][P],
-                                          f2 (&cacc)[4][P], f2& r2, f2& prod, float& l1) {
+__device__ __forceinline__ void pair_unit(const PairOperandsF32<P>& o, const f2 (&nxj)[4][P], int i0, int j0, int n,
+                                          int lane, const PairConstsF32& k, f2 (&racc)[2][P], f2 (&cacc)[4][P],
+                                          f2& r2, f2& prod, float& l1) {
     f2 prodm = pk(1.f, 1.f);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const float4 b = *reinterpret_cast<const float4*>(sBl + c * (32 * kPairRows));
+        const float4 b = o.b[c];
         const int j = j0 + lane + 32 * c;
 #pragma unroll
         for (int rp = 0; rp < 2; ++rp) {
-            const float a0 = sA[(4 * wr + 2 * rp) * kPairCols + lane + 32 * c];
-            const float a1 = sA[(4 * wr + 2 * rp + 1) * kPairCols + lane + 32 * c];
+            float a0, a1;
+            upk(o.a[c][rp], a0, a1);
             const float b0 = rp == 0 ? b.x : b.z;
             const float b1 = rp == 0 ? b.y : b.w;
             bool vA0 = true, vA1 = true, vB0 = true, vB1 = true;
@@ -241,7 +283,7 @@ __device__ __forceinline__ void pair_unit(const float* __restrict__ sA, const fl
                 vB0 = ok0 && (b0 == b0);
                 vB1 = ok1 && (b1 == b1);
             }
-            pair_pack<P, TRUNC, MASKED>(xi[rp], nxj[c], pk(a0, a1), pk(b0, b1), vA0, vA1, vB0, vB1, k, racc[rp],
+            pair_pack<P, TRUNC, MASKED>(o.xi[rp], nxj[c], o.a[c][rp], pk(b0, b1), vA0, vA1, vB0, vB1, k, racc[rp],
                                         cacc[c], r2, prod, prodm);
         }
     }
@@ -280,6 +322,11 @@ struct PairMathF32 {
     using S = float;     // delta element
     using Part = float;  // row and column partials
     static constexpr bool kXJEveryUnit = false;  // x_J is copied with the first unit of each block only
+    // The warp copies its operands of a unit into registers and releases the
+    // stage before the pair math, so the next copy into it can start a unit
+    // earlier (the ring runs one more unit ahead of the consumers).
+    static constexpr bool kEarlyRelease = MDSX_PAIR_EARLY_RELEASE != 0;
+    using Operands = PairOperandsF32<P>;
     static constexpr int kFoldUnits = 4;  // r^2 pack: 16 terms per half per unit; 1/Phi product: 8 factors
     struct Cols {        // one column block: negated (x_j, x_j) packs and the column sums
         f2 nxj[4][P];
@@ -313,27 +360,28 @@ struct PairMathF32 {
                 cols.acc[c][q] = pk(0.f, 0.f);
             }
     }
-    // One unit: v[r * P + q] = this lane's sum of the (i, j) terms of row 4w + r.
+    __device__ static void load(Operands& o, const S* sA, const S* sB, const X* sXI, int lane, int warp) {
+        pair_load_f32<P>(o, sA, sB, sXI, lane, warp);
+    }
+    // One unit from its operands: v[r * P + q] = this lane's sum of the (i, j) terms of row 4w + r.
     template <bool MASKED>
-    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
-                         int lane, int warp, Part (&v)[4 * P]) const {
-        // this lane's 16-byte chunk (rows 4w .. 4w+3) of B row `lane`, 128-byte swizzle:
-        // chunk c of a 128-byte row r sits at chunk c ^ (r & 7)
-        const float* sBl = sB + lane * kPairRows + ((warp ^ (lane & 7)) << 2);
-        f2 xi[2][P], racc[2][P];
+    __device__ void compute(const Operands& o, Cols& cols, Sums& s, int i0, int j0, int n, int lane,
+                            Part (&v)[4 * P]) const {
+        f2 racc[2][P];
 #pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const float4 x4 = *reinterpret_cast<const float4*>(sXI + q * kPairRows + 4 * warp);
-            xi[0][q] = pk(x4.x, x4.y);
-            xi[1][q] = pk(x4.z, x4.w);
-            racc[0][q] = racc[1][q] = pk(0.f, 0.f);
-        }
-        pair_unit<P, TRUNC, MASKED>(sA, sBl, xi, cols.nxj, i0, j0, n, lane, warp, k, racc, cols.acc, s.r2, s.prod,
-                                    s.l1);
+        for (int q = 0; q < P; ++q) racc[0][q] = racc[1][q] = pk(0.f, 0.f);
+        pair_unit<P, TRUNC, MASKED>(o, cols.nxj, i0, j0, n, lane, k, racc, cols.acc, s.r2, s.prod, s.l1);
 #pragma unroll
         for (int rp = 0; rp < 2; ++rp)
 #pragma unroll
             for (int q = 0; q < P; ++q) upk(racc[rp][q], v[(2 * rp) * P + q], v[(2 * rp + 1) * P + q]);
+    }
+    template <bool MASKED>
+    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
+                         int lane, int warp, Part (&v)[4 * P]) const {
+        Operands o;
+        load(o, sA, sB, sXI, lane, warp);
+        compute<MASKED>(o, cols, s, i0, j0, n, lane, v);
     }
     __device__ static void after_unit(Sums& s) {
         if (++s.since_fold == kFoldUnits) {
@@ -363,6 +411,7 @@ struct PairMathF32Cols {
     using Part = float;
     static constexpr int kFoldUnits = 4;  // per half: 16 r^2 terms and 8 factors of 1/Phi per unit
     static constexpr bool kXJEveryUnit = true;
+    static constexpr bool kEarlyRelease = false;  // reads its operands from the stage during the math
     struct Cols {
         f2 acc[2][P];  // column sums of columns (l + 64 cp, l + 64 cp + 32)
     };
@@ -510,6 +559,7 @@ struct PairMathF64 {
     using S = DeltaT;  // float (DELTA_F32 mode) or double (FP64 mode)
     using Part = double;
     static constexpr bool kXJEveryUnit = false;
+    static constexpr bool kEarlyRelease = false;  // bound by the FP64 pipe: reads its operands from the stage
     static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
         double xj[4][P];
@@ -649,12 +699,23 @@ __device__ __forceinline__ bool pair_consume_unit(const M& math, typename M::Sum
     const int i0 = I * kPairRows + 4 * warp;
     const int j0 = J * kPairCols;
     typename M::Part v[4 * P];
-    if (masked)
-        math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
-    else
-        math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[stage]);
+    if constexpr (M::kEarlyRelease) {
+        typename M::Operands o;
+        M::load(o, sA, sB, sXI, lane, warp);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[stage]);
+        if (masked)
+            math.template compute<true>(o, cols, sums, i0, j0, n, lane, v);
+        else
+            math.template compute<false>(o, cols, sums, i0, j0, n, lane, v);
+    } else {
+        if (masked)
+            math.template unit<true>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
+        else
+            math.template unit<false>(sA, sB, sXI, cols, sums, i0, j0, n, lane, warp, v);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[stage]);
+    }
     // row sums of this unit: rows 4w .. 4w+3, value index r * P + q
     flush_row_sums<4 * P>(v, rowpart_unit + (size_t)(4 * warp) * P, lane);
     M::after_unit(sums);
@@ -697,7 +758,7 @@ __device__ __forceinline__ void pair_flush_likelihood(typename M::Sums& sums, do
 // P = 3 0.336 / 0.385 ms, P = 4 0.429 / 0.400, P = 5 0.423 / 0.449, P = 6 0.77 / 0.49.
 template <int P>
 constexpr int pair_min_ctas() {
-    return (P == 4 || P == 6) ? 1 : 2;
+    return (P == 4 || P == 6) ? 1 : MDSX_PAIR_F32_CTAS;
 }
 
 // FP64 pair math runs one CTA per SM at up to 255 registers: the FP64 pipe bounds
