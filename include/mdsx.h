@@ -292,6 +292,11 @@ typedef struct {
     size_t resume_bytes;
     void* checkpoint;
     size_t checkpoint_capacity;
+    /* Nonzero: during burn-in the half-width of the precision proposal adapts
+     * toward 44 % acceptance (log half-width += (accepted - 0.44) / sqrt(t)),
+     * then stays fixed. The reference keeps it at 0.01, which at N = 50 000
+     * moves tau far too slowly; off by default. */
+    int adapt_precision_proposal;
 } mdsx_hmc_config;
 
 #define MDSX_HMC_CHECKPOINT_BYTES(n, p) \

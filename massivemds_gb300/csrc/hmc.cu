@@ -627,7 +627,8 @@ struct CkptHeader {
     int64_t next_iteration;
     double tau, eps, hbar, log_eps_bar, loglik0, logprior0, u0;
     int32_t rng_len, pad;
-    int64_t reserved[2];
+    double precision_half_width;  // the precision proposal's (adapted) half-width
+    int64_t reserved;
 };
 static_assert(sizeof(CkptHeader) == 112, "checkpoint header layout");
 
@@ -736,12 +737,14 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
     c.rng.seed(cfg->seed ^ 0x5DEECE66DULL);
     c.eps = cfg->step_size;
     const long long it0 = cfg->resume ? resume_state.h.next_iteration : 0;
+    double tau_hw = cfg->precision_half_width;  // the precision proposal's half-width (adapted in burn-in)
     if (cfg->resume) {
         std::istringstream in(resume_state.rng);
         in >> c.rng;
         if (in.fail()) return fail(e, MDSX_EINVAL, "hmc: checkpoint holds a bad generator state");
         c.eps = resume_state.h.eps;
         e->tau = resume_state.h.tau;
+        if (resume_state.h.precision_half_width > 0.0) tau_hw = resume_state.h.precision_half_width;
         e->sum_known = e->grad_known = false;
     }
     int rc = c.alloc();
@@ -913,8 +916,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         // Metropolis step on the precision (R/Untitled.R:668-691)
         if (cfg->learn_precision) {
             const double tau_old = e->tau;
-            const double tau_new =
-                std::fabs(tau_old + cfg->precision_half_width * (2.0 * unif(c.rng) - 1.0));
+            const double tau_new = std::fabs(tau_old + tau_hw * (2.0 * unif(c.rng) - 1.0));
             MDSX_CUDA(e, mdsx::convert_locations(c.x0, n, p, e->d_x[e->xcur], e->x_ld, e->x_f32, c.s));
             e->tau = tau_new;
             double loglik_t = 0.0;
@@ -923,7 +925,13 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
                 return rc;
             }
             const double u_t = -(loglik_t + logprior0);
-            if (std::isfinite(u_t) && std::log(unif(c.rng)) < u0 - u_t) {
+            const bool tau_accept = std::isfinite(u_t) && std::log(unif(c.rng)) < u0 - u_t;
+            if (cfg->adapt_precision_proposal && it < cfg->burn_in) {
+                // Robbins-Monro on the log half-width toward 44 % acceptance (diminishing steps)
+                tau_hw *= std::exp(((tau_accept ? 1.0 : 0.0) - 0.44) / std::sqrt((double)it + 1.0));
+                tau_hw = std::min(std::max(tau_hw, 1e-12), 1e12);
+            }
+            if (tau_accept) {
                 loglik0 = loglik_t;
                 u0 = u_t;
                 MDSX_CUDA(e, cudaMemcpyAsync(c.gl0, e->d_grad[e->gcur], (size_t)n * p * sizeof(double),
@@ -996,6 +1004,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
         out.h.loglik0 = loglik0;
         out.h.logprior0 = logprior0;
         out.h.u0 = u0;
+        out.h.precision_half_width = tau_hw;
         out.s0 = s0;
         out.lambda.assign(c.lam.m, c.lam.m + p * p);
         out.x0.resize((size_t)n * p);

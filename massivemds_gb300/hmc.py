@@ -51,6 +51,7 @@ class _Config(ctypes.Structure):
         ("resume_bytes", ctypes.c_size_t),
         ("checkpoint", ctypes.c_void_p),
         ("checkpoint_capacity", ctypes.c_size_t),
+        ("adapt_precision_proposal", ctypes.c_int),
     ]
 
 
@@ -104,7 +105,7 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
         seed: int = 666, traced_pairs=None, traced_locations=None, use_graph: bool = True, surrogate=None,
         harvest_iterations: int = 0, harvest_start: int | None = None, harvest_rows: int = 100, train_steps: int = 2000, train_batch: int = 512,
         train_learning_rate: float = 1e-3, fallback_accept: float = 0.6, fallback_window: int = 50,
-        checkpoint: bool = False, resume: bytes | None = None) -> HmcResult:
+        checkpoint: bool = False, resume: bytes | None = None, adapt_precision_proposal: bool = False) -> HmcResult:
     """Runs one chain on the engine's GPU; the engine must hold delta and tau.
 
     Defaults follow the reference: 20 leapfrog steps of 0.01 (trajectory 0.2,
@@ -117,6 +118,10 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
     with the exact potential deciding every accept, until the acceptance over
     the last ``fallback_window`` surrogate iterations drops below
     ``fallback_accept`` (exact gradients from then on).
+
+    ``adapt_precision_proposal=True`` adapts the precision proposal's
+    half-width toward 44 % acceptance during burn-in (the reference keeps
+    ``precision_half_width`` fixed).
 
     ``checkpoint=True`` returns the chain's state after its last iteration in
     ``HmcResult.checkpoint``; ``resume=<those bytes>`` (same engine, delta and
@@ -145,6 +150,7 @@ def hmc(engine: Engine, initial_locations, iterations: int, burn_in: int = 0, le
     cfg.resume_bytes = len(resume) if resume is not None else 0
     cfg.checkpoint = ctypes.cast(ckpt_buf, ctypes.c_void_p) if ckpt_buf is not None else None
     cfg.checkpoint_capacity = cap
+    cfg.adapt_precision_proposal = int(adapt_precision_proposal)
     cols = TRACE_BASE + len(pairs) + len(locs)
     trace = np.empty((iterations, cols), dtype=np.float64)
     final = np.empty((n, p), dtype=np.float64)

@@ -11,6 +11,14 @@ classical-MDS start, the step size tuned toward 0.8 acceptance over the first
 potential. The synthetic delta and the start are built on the GPU with torch
 (host copies only for the engine's setPairwiseData).
 
+By default the half-width of the tau proposal adapts toward 44 % acceptance
+during burn-in (the reference's fixed 0.01 moves tau too slowly at this N;
+--fixed-precision-proposal keeps it). With --surrogate a second chain from the
+same start runs with the learned gradient surrogate (K = 512 landmarks, MLP of
+3 hidden layers of width 512, trained on rows harvested during burn-in; exact
+potential at every accept; fallback to exact gradients below 0.6 acceptance),
+and both chains' min ESS/s are reported side by side.
+
 Prints one JSON line: seconds per iteration, fused sweeps per second and the
 bytes they read, acceptance, the learned tau, min ESS over invariant
 functionals (tau included) and min ESS/s.
@@ -26,6 +34,7 @@ import torch
 
 from . import Engine, diagnostics, flags as F
 from .hmc import hmc
+from .surrogate import Surrogate
 
 
 def make_delta(n: int, dim: int, noise_sd: float, seed: int, dev) -> torch.Tensor:
@@ -97,6 +106,13 @@ def main(argv=None):
     ap.add_argument("--burn-in", type=int, default=200)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--seed", type=int, default=11)
+    ap.add_argument("--fixed-precision-proposal", action="store_true",
+                    help="keep the reference's tau proposal half-width 0.01 throughout")
+    ap.add_argument("--surrogate", action="store_true", help="also run the surrogate-gradient chain")
+    ap.add_argument("--landmarks", type=int, default=512)
+    ap.add_argument("--width", type=int, default=512)
+    ap.add_argument("--layers", type=int, default=3)
+    ap.add_argument("--harvest-rows", type=int, default=250)
     args = ap.parse_args(argv)
 
     dev = torch.device("cuda", 0)
@@ -117,11 +133,31 @@ def main(argv=None):
     pairs = rng.integers(0, args.n, (50, 2))
     pairs = pairs[pairs[:, 0] != pairs[:, 1]]
     locs = rng.choice(args.n, 50, replace=False)
+    common = dict(iterations=args.iterations, burn_in=args.burn_in, leapfrog_steps=args.steps, step_size=1e-3,
+                  adapt_step_size=True, target_accept=0.8, learn_precision=True, precision_half_width=0.01,
+                  adapt_precision_proposal=not args.fixed_precision_proposal, learn_trait_precision=True,
+                  seed=args.seed, traced_pairs=pairs, traced_locations=locs)
     t = time.time()
-    res = hmc(e, x0, iterations=args.iterations, burn_in=args.burn_in, leapfrog_steps=args.steps, step_size=1e-3,
-              adapt_step_size=True, target_accept=0.8, learn_precision=True, precision_half_width=0.01,
-              learn_trait_precision=True, seed=args.seed, traced_pairs=pairs, traced_locations=locs)
+    res = hmc(e, x0, **common)
     wall = time.time() - t
+    sur_out = None
+    if args.surrogate:
+        e.setParameters([tau0])
+        s = Surrogate(e, landmarks=args.landmarks, width=args.width, layers=args.layers,
+                      max_training_rows=(args.burn_in - args.burn_in // 2) * args.harvest_rows, seed=args.seed)
+        t = time.time()
+        sres = hmc(e, x0, surrogate=s, harvest_iterations=args.burn_in, harvest_start=args.burn_in // 2,
+                   harvest_rows=args.harvest_rows, train_steps=4000, train_batch=512, train_learning_rate=1e-3,
+                   fallback_accept=0.6, fallback_window=50, **common)
+        s_wall = time.time() - t
+        s.close()
+        scols = diagnostics.invariant_functionals(sres, include_precision=True)[args.burn_in:]
+        s_mess, _ = diagnostics.min_ess(scols)
+        sur_out = {"min_ess": s_mess, "min_ess_per_s": s_mess / sres.seconds, "seconds": sres.seconds,
+                   "accept": sres.accept_rate, "fallback_iteration": sres.fallback_iteration,
+                   "train_seconds": sres.train_seconds, "train_loss": sres.train_loss,
+                   "surrogate_evaluations": sres.surrogate_evaluations, "wall_seconds": s_wall,
+                   "tau_final": sres.precision}
     e.close()
     kept = args.iterations - args.burn_in
     cols = diagnostics.invariant_functionals(res, include_precision=True)[args.burn_in:]
@@ -147,6 +183,10 @@ def main(argv=None):
         "min_ess": mess,
         "min_ess_functional": int(k),
         "min_ess_per_s": mess / res.seconds,
+        "precision_proposal": "fixed 0.01" if args.fixed_precision_proposal else "adapted in burn-in",
+        "tau_accept": float(np.mean(tau_chain[1:] != tau_chain[:-1])),
+        "surrogate": sur_out,
+        "ratio": (sur_out["min_ess_per_s"] / (mess / res.seconds)) if sur_out else None,
     }
     print(json.dumps(out))
 

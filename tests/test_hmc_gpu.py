@@ -161,3 +161,27 @@ def test_resume_rejects_a_foreign_checkpoint():
     with pytest.raises(MdsxError):
         hmc(e3, np.zeros((n, 3)), iterations=3, step_size=0.003, seed=1, resume=first.checkpoint)  # P differs
     e3.close()
+
+
+def test_precision_proposal_adapts_during_burn_in():
+    """With adapt_precision_proposal the half-width of the tau proposal moves
+    toward 44 % acceptance during burn-in and is then fixed (read back from the
+    checkpoint header); without it the half-width stays the reference's."""
+    import struct
+
+    n, p = 150, 2
+    delta, x0 = _problem(n, p, 12, clusters=3)
+    out = {}
+    for adapt in (False, True):
+        e = _engine(delta, p, 0.2, 0)  # tau far from its posterior
+        res = hmc(e, x0, iterations=400, burn_in=300, leapfrog_steps=5, step_size=0.003, adapt_step_size=True,
+                  learn_precision=True, precision_half_width=0.01, seed=4, checkpoint=True,
+                  adapt_precision_proposal=adapt)
+        e.close()
+        hw = struct.unpack_from("<d", res.checkpoint, 96)[0]
+        tau = res.column("precision")
+        moves = float(np.mean(tau[301:] != tau[300:-1]))
+        out[adapt] = (hw, moves)
+    assert out[False][0] == 0.01
+    assert out[True][0] != 0.01
+    assert 0.15 < out[True][1] < 0.8, out  # the adapted proposal accepts a fair share of moves
