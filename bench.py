@@ -88,7 +88,7 @@ def parse():
                          "the sum and all-gather of the gradient rows every evaluation)")
     ap.add_argument("--cpu-seconds", type=float, default=3.0,
                     help="wall time of each bounded CPU row sample (one-core and FP32 paths)")
-    ap.add_argument("--sections", default="parity,f64,c1,c3",
+    ap.add_argument("--sections", default="parity,f64,noalloc,c1,c3",
                     help="comma list of the headline line's extra sections to run ('' for none)")
     return ap.parse_args()
 
@@ -514,6 +514,77 @@ def measure_c3(local, steps, warmup, check=3):
 
 # --------------------------------------------------------------- headline
 
+def measure_noalloc(local, delta, xs, refs, calls=20, warmup=3):
+    """The allocation-free FP32 sweep (mdsx_sweep_f32_noalloc: static scratch,
+    caller-owned device buffers, synchronous) against the engine's row-block
+    FP32 sweep, the kernel it runs, on the same delta: GPU time per call from
+    CUDA events on the call's stream (the call's own host synchronisation
+    inside the window), and the results at the checked states against the
+    oracle."""
+    import numpy as np
+    import torch
+
+    import massivemds_gb300 as m
+    from massivemds_gb300._lib import load
+
+    lib = load()
+    n = delta.shape[0]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    ddelta = torch.from_numpy(delta).to(dev)  # row stride N (a multiple of 4 floats)
+    pool = torch.from_numpy(np.ascontiguousarray(xs)).to(dev)
+    out_sum = torch.zeros(1, dtype=torch.float64, device=dev)
+    out_grad = torch.zeros(n * P, dtype=torch.float64, device=dev)
+
+    def call(k):
+        rc = lib.mdsx_sweep_f32_noalloc(ddelta.data_ptr(), n, pool[k % len(xs)].data_ptr(), n, P, TAU, 1,
+                                        out_sum.data_ptr(), out_grad.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(lib.mdsx_last_error(None).decode())
+
+    def events_ms(fn):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(calls)]
+        for k in range(calls):
+            ev[k][0].record(stream)
+            fn(k)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        return statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+    for k in range(warmup):
+        call(k)
+    noalloc_ms = events_ms(call)
+    worst_s = worst_g = 0.0
+    for k, (s_ref, g_ref) in enumerate(refs):
+        call(k)
+        torch.cuda.synchronize()
+        worst_s = max(worst_s, rel(float(out_sum.item()), s_ref))
+        worst_g = max(worst_g, grad_rel(out_grad.cpu().numpy(), g_ref))
+    eng = m.Engine(P, n, m.flags.FLOAT | m.flags.LEFT_TRUNCATION, local)
+    eng.set_sweep_schedule(m.flags.SWEEP_ROWS)
+    eng.setPairwiseData(delta)
+    eng.setParameters([TAU])
+    eng.set_stream(stream.cuda_stream)
+
+    def engine_call(k):
+        eng.update_locations_device(pool[k % len(xs)].data_ptr())
+        eng.evaluate_device(out_sum.data_ptr(), out_grad.data_ptr())
+
+    for k in range(warmup):
+        engine_call(k)
+    torch.cuda.synchronize()
+    engine_ms = events_ms(engine_call)
+    eng.set_stream(None)
+    eng.close()
+    del ddelta
+    return {"ms_per_call": noalloc_ms, "engine_rows_ms": engine_ms, "ratio": noalloc_ms / engine_ms,
+            "what": "one synchronous mdsx_sweep_f32_noalloc call (location conversion, padding-row marks, "
+                    "row-block sweep, results to the caller's buffers) against the engine's location update + "
+                    "row-block evaluation with its results copied out, CUDA events, N=20000 FP32",
+            "parity": {"sum_rel_max": worst_s, "grad_rel_max": worst_g, "calls_checked": len(refs),
+                       "tolerance": PARITY_TOL["f32"]}}
+
+
 def measure_f64(local, delta, xs, refs, steps=10, warmup=3):
     """FP64 pair arithmetic over the FP32-stored delta (DELTA_F32): evals/s and
     the sweep's kernel time; the FP64 results at the checked states against
@@ -824,7 +895,7 @@ def run_mdsx(args):
                              "sample": f"one whole evaluation (all {n} rows: likelihood pass + gradient pass), "
                                        f"{cpu_s:.2f} s", "paths": paths},
         }
-        if "parity" in sections or "f64" in sections:
+        if "parity" in sections or "f64" in sections or "noalloc" in sections:
             xs = pool_np[check_idx]
             refs = oracle_states(delta, xs, TAU)
             if "parity" in sections:
@@ -837,6 +908,8 @@ def run_mdsx(args):
                     "sums_finite": int(np.isfinite(timed_sums).sum()), "tolerance": [tol_s, tol_g]}
             if "f64" in sections and not f64:
                 line["f64"] = measure_f64(local, delta, xs, refs)
+            if "noalloc" in sections and not f64 and n <= 32768:
+                line["noalloc"] = measure_noalloc(local, delta, xs, refs)
         del delta
         if "c1" in sections:
             line["c1"] = measure_c1(local, steps=5, warmup=3)

@@ -74,6 +74,25 @@ int scratch_address(void** out) {
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
+// One launch for a call's preparation: zero the sums, the error word and the
+// counters; mark the padding rows (>= N) for the masked path and clear the
+// others; convert the locations to the FP32 SoA layout [P][x_ld].
+__global__ void noalloc_prepare_kernel(double* __restrict__ out, unsigned* __restrict__ counts, int n_counts,
+                                       int* __restrict__ row_nan, int n, int rows_padded,
+                                       const double* __restrict__ locations, int p, float* __restrict__ x, int x_ld) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t0 < 4) out[t0] = 0.0;
+    for (long long i = t0; i < n_counts; i += stride) counts[i] = 0u;
+    for (long long i = t0; i < rows_padded; i += stride) row_nan[i] = i >= n ? 1 : 0;
+    const long long total = (long long)p * x_ld;
+    for (long long idx = t0; idx < total; idx += stride) {
+        const int q = (int)(idx / x_ld);
+        const int i = (int)(idx - (long long)q * x_ld);
+        x[idx] = i < n ? (float)locations[(long long)i * p + q] : 0.0f;
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -166,9 +185,14 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
         return noalloc_fail(MDSX_EINVAL, "problem needs " + std::to_string(off) + " bytes of scratch; the allocation-free "
                             "sweep has " + std::to_string(kNoAllocScratchBytes));
 
-    NOALLOC_CUDA(mdsx::convert_locations(d_locations, n, p, x, x_ld, true, stream));
     // First pass: only the padding rows (>= N) take the masked path.
-    NOALLOC_CUDA(mdsx::mark_padding_rows(n, row_nan, rows_padded, stream));
+    {
+        const long long work = std::max<long long>((long long)p * x_ld, rows_padded);
+        const int blocks = (int)std::min<long long>((work + 255) / 256, 1024);
+        noalloc_prepare_kernel<<<blocks, 256, 0, stream>>>(out, counts, n_row_blocks + 1, row_nan, n, rows_padded,
+                                                           d_locations, p, x, x_ld);
+        NOALLOC_CUDA(cudaGetLastError());
+    }
 
     CUtensorMap tmap_delta{}, tmap_x{};
     rc = tmap_f32(&tmap_delta, d_delta, n, n, delta_ld, mdsx::kStepCols, rb);
@@ -209,12 +233,17 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
     a.sums_out = out;
     a.truncation = truncation ? 1 : 0;
     a.err = reinterpret_cast<int*>(out + 3);
-    // Counters, sums and the error word must start at zero on each pass.
+    // Counters, sums and the error word start at zero on each pass (the
+    // preparation kernel clears them for the first).
     double host_out[4];
     for (int pass = 0; pass < 2; ++pass) {
-        NOALLOC_CUDA(cudaMemsetAsync(out, 0, 4 * sizeof(double), stream));
-        NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
+        if (pass == 1) {  // the second pass starts from zero again
+            NOALLOC_CUDA(cudaMemsetAsync(out, 0, 4 * sizeof(double), stream));
+            NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
+        }
         NOALLOC_CUDA(mdsx::sweep_launch(mdsx::Mode::kF32, p, truncation != 0, grid, tmap_delta, tmap_x, a, stream));
+        // the sum to the caller and the status to the host, then one synchronisation
+        NOALLOC_CUDA(cudaMemcpyAsync(d_sum_of_increments, out + 2, sizeof(double), cudaMemcpyDeviceToDevice, stream));
         NOALLOC_CUDA(cudaMemcpyAsync(host_out, out, sizeof(host_out), cudaMemcpyDeviceToHost, stream));
         NOALLOC_CUDA(cudaStreamSynchronize(stream));
         int dev_err = 0;
@@ -225,8 +254,6 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
         if (!std::isnan(host_out[2]) || pass == 1) break;
         NOALLOC_CUDA(mdsx::mark_nan_rows(d_delta, true, n, delta_ld, row_nan, rows_padded, stream));
     }
-    NOALLOC_CUDA(cudaMemcpyAsync(d_sum_of_increments, out + 2, sizeof(double), cudaMemcpyDeviceToDevice, stream));
-    NOALLOC_CUDA(cudaStreamSynchronize(stream));
     return MDSX_OK;
 }
 

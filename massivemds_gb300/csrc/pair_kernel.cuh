@@ -57,13 +57,19 @@ constexpr int kPairCols = 128;  // columns per block J: 32 lanes x 4
 constexpr int kPairRows = 32;   // rows per chunk I: 8 warps x 4
 constexpr int kPairWarps = 8;
 constexpr int kPairThreads = kPairWarps * 32;
-constexpr int kPairMaxP = 6;     // FP32 pair math: P <= 4 row packs (PairMathF32), 5..6 column packs
+constexpr int kPairMaxP = 6;     // FP32 pair math: packs of two rows (PairMathF32), or of two columns (PairMathF32Cols) above MDSX_PAIR_ROWPACK_MAX_P
 constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_ctas_of)
 #ifndef MDSX_PAIR_F32_STAGES
 #define MDSX_PAIR_F32_STAGES 3  // TMA ring depth of the FP32 pair kernels
 #endif
 #ifndef MDSX_PAIR_F32_CTAS
 #define MDSX_PAIR_F32_CTAS 2  // CTAs per SM of the FP32 pair kernels with P = 1, 2, 3, 5
+#endif
+#ifndef MDSX_FINISH_THREADS
+#define MDSX_FINISH_THREADS 512  // threads per block of the pair sweep's finish kernel
+#endif
+#ifndef MDSX_FINISH_CHUNK
+#define MDSX_FINISH_CHUNK 8  // row-partial loads in flight per finish thread
 #endif
 #ifndef MDSX_PAIR_EARLY_RELEASE
 #define MDSX_PAIR_EARLY_RELEASE 1  // FP32 packs of rows: operands to registers, stage released before the math
@@ -494,9 +500,12 @@ struct PairMathF32Cols {
 };
 
 // The FP32 policy for P.
+#ifndef MDSX_PAIR_ROWPACK_MAX_P
+#define MDSX_PAIR_ROWPACK_MAX_P 6  // FP32: packs of two rows up to this P, packs of two columns above
+#endif
 template <int P, bool TRUNC>
 using PairMathF32For =
-    typename std::conditional<(P <= 4), PairMathF32<P, TRUNC>, PairMathF32Cols<P, TRUNC>>::type;
+    typename std::conditional<(P <= MDSX_PAIR_ROWPACK_MAX_P), PairMathF32<P, TRUNC>, PairMathF32Cols<P, TRUNC>>::type;
 
 // ------------------------------------------------------------ FP64 pair math
 
@@ -758,7 +767,7 @@ __device__ __forceinline__ void pair_flush_likelihood(typename M::Sums& sums, do
 // P = 3 0.336 / 0.385 ms, P = 4 0.429 / 0.400, P = 5 0.423 / 0.449, P = 6 0.77 / 0.49.
 template <int P>
 constexpr int pair_min_ctas() {
-    return (P == 4 || P == 6) ? 1 : MDSX_PAIR_F32_CTAS;
+    return (P >= 4 && P <= MDSX_PAIR_ROWPACK_MAX_P) || P == 6 ? 1 : MDSX_PAIR_F32_CTAS;
 }
 
 // FP64 pair math runs one CTA per SM at up to 255 registers: the FP64 pipe bounds
@@ -921,10 +930,10 @@ __device__ __forceinline__ T tree_sum(T (&v)[K]) {
 
 template <int P>
 struct FinishShape {
-    static constexpr int kThreads = 512;
+    static constexpr int kThreads = MDSX_FINISH_THREADS;
     static constexpr int kOut = kPairRows * P;       // outputs per row chunk
     static constexpr int kGroups = kThreads / kOut;  // P = 1: 16, 2: 8, 3: 5, 4: 4
-    static constexpr int kChunk = 8;                 // loads in flight per thread
+    static constexpr int kChunk = MDSX_FINISH_CHUNK;  // loads in flight per thread
 };
 
 // Block `blk` of the finish of one sweep (block 0: likelihood; block nc - I: row chunk I).
@@ -1051,7 +1060,7 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
 }
 
 template <int P, typename Part>
-__global__ void __launch_bounds__(512) pair_finish_kernel(const PairArgs a) {
+__global__ void __launch_bounds__(MDSX_FINISH_THREADS) pair_finish_kernel(const PairArgs a) {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     pair_finish_block<P, Part>(a, (int)blockIdx.x);
 }
