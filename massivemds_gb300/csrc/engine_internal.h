@@ -50,6 +50,14 @@ struct mdsx_engine {
     unsigned* d_counts = nullptr;  // [n_row_blocks] + [1]
     int* d_row_nan = nullptr;
     double* h_out = nullptr;  // pinned mirror of d_out
+    // Small problems only (null otherwise): pinned staging of a caller's host
+    // locations (N*P doubles), so that updateLocations returns without waiting
+    // for the device (h2d_done marks the end of the last copy out of it), and a
+    // pinned mirror of the gradient (rows*P doubles), brought to the host in the
+    // same wait as the sums so that getLogLikelihoodGradient needs no second one.
+    double* h_xstage = nullptr;
+    double* h_grad = nullptr;
+    bool h_grad_valid = false;  // h_grad holds d_grad[gcur] as of the last sweep_and_read
 
     CUtensorMap tmap_delta{};
     CUtensorMap tmap_x[2]{};
