@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas<P>()) batch_pair_k
 // The finish of every instance: block b belongs to the instance whose
 // finish_begin is the largest <= b.
 template <int P>
-__global__ void __launch_bounds__(FinishShape<P>::kThreads) batch_pair_finish_kernel(const BatchPairArgs ba) {
+__global__ void __launch_bounds__(FinishShape<P, float>::kThreads) batch_pair_finish_kernel(const BatchPairArgs ba) {
+    static_assert(pair_finish_blocks<P, float>(1) == 2, "the batch plans nc + 1 finish blocks per instance");
     asm volatile("griddepcontrol.wait;" ::: "memory");
     int lo = 0, hi = ba.count - 1;
     const int b = (int)blockIdx.x;

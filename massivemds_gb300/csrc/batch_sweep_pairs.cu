@@ -29,7 +29,7 @@ cudaError_t launch_pairs_one(const BatchPairArgs& a, int grid, int finish_blocks
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3((unsigned)finish_blocks);
-    cfg.blockDim = dim3(FinishShape<P>::kThreads);
+    cfg.blockDim = dim3(FinishShape<P, float>::kThreads);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

@@ -66,13 +66,19 @@ constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_cta
 #define MDSX_PAIR_F32_CTAS 2  // CTAs per SM of the FP32 pair kernels with P = 1, 2, 3, 5
 #endif
 #ifndef MDSX_FINISH_THREADS
-#define MDSX_FINISH_THREADS 512  // threads per block of the pair sweep's finish kernel (P > MDSX_FINISH_SMALL_P)
+#define MDSX_FINISH_THREADS 256  // threads per block of the pair sweep's finish kernel (P > MDSX_FINISH_SMALL_P)
 #endif
 #ifndef MDSX_FINISH_THREADS_SMALL_P
-#define MDSX_FINISH_THREADS_SMALL_P 256  // the same for P <= MDSX_FINISH_SMALL_P
+#define MDSX_FINISH_THREADS_SMALL_P 128  // the same for P <= MDSX_FINISH_SMALL_P
 #endif
 #ifndef MDSX_FINISH_SMALL_P
-#define MDSX_FINISH_SMALL_P 3
+#define MDSX_FINISH_SMALL_P 2
+#endif
+#ifndef MDSX_FINISH_THREADS_F64
+#define MDSX_FINISH_THREADS_F64 512  // the same for FP64 partials, every P
+#endif
+#ifndef MDSX_FINISH_SPLIT_F64
+#define MDSX_FINISH_SPLIT_F64 4  // FP64 partials: finish blocks per row chunk
 #endif
 #ifndef MDSX_FINISH_CHUNK
 #define MDSX_FINISH_CHUNK 8  // row-partial loads in flight per finish thread
@@ -934,22 +940,39 @@ __device__ __forceinline__ T tree_sum(T (&v)[K]) {
     return v[0];
 }
 
-template <int P>
+template <int P, typename Part>
 struct FinishShape {
-    // Measured on GB300 (FP32, truncated): 256-thread blocks for P <= 3 fit every
-    // block of the finish in one wave (N = 20 000: 626 blocks) and take
-    // 0.5 % (N = 20 000) to 2 % (N = 5 000) off an evaluation against 512.
-    static constexpr int kThreads = P <= MDSX_FINISH_SMALL_P ? MDSX_FINISH_THREADS_SMALL_P : MDSX_FINISH_THREADS;
-    static constexpr int kOut = kPairRows * P;       // outputs per row chunk
-    static constexpr int kGroups = kThreads / kOut;  // P = 1: 8, 2: 4, 3: 2, 4: 4, 5: 3, 6: 2
+    // FP32 partials: small blocks. That finish is latency-bound (a few dependent
+    // rounds of partial loads per block), so more resident blocks beat more
+    // threads per block. Measured on GB300 (FP32, truncated) against 512 threads
+    // for every P: the 64-instance batch 1.428 -> 1.339 ms, N = 20 000 evaluation
+    // -0.5 % (P = 2) and -0.8 % (P = 6). FP64 partials: 512 threads, as the
+    // blocks of the first column blocks are bound by FP64 adds (N = 1000, P = 2:
+    // 9.2 us against 12.3 us with 128 threads).
+    static constexpr int kThreads = sizeof(Part) == 8             ? MDSX_FINISH_THREADS_F64
+                                    : P <= MDSX_FINISH_SMALL_P ? MDSX_FINISH_THREADS_SMALL_P
+                                                               : MDSX_FINISH_THREADS;
+    // FP64 partials: each row chunk is split over kSplit blocks of kRows rows, so
+    // that the FP64 adds of a chunk's column partials spread over kSplit SMs.
+    static constexpr int kSplit = sizeof(Part) == 8 ? MDSX_FINISH_SPLIT_F64 : 1;
+    static constexpr int kRows = kPairRows / kSplit;  // rows per block
+    static constexpr int kOut = kRows * P;            // outputs per block
+    static constexpr int kGroups = kThreads / kOut;   // FP32: P = 1: 4, 2: 2, 3: 2, 4: 2, 5: 1, 6: 1
     static_assert(kGroups >= 1, "a finish block must hold one row chunk's outputs");
     static constexpr int kChunk = MDSX_FINISH_CHUNK;  // loads in flight per thread
 };
 
-// Block `blk` of the finish of one sweep (block 0: likelihood; block nc - I: row chunk I).
+// Finish blocks of one sweep: the likelihood block and kSplit per row chunk.
+template <int P, typename Part>
+__host__ __device__ constexpr int pair_finish_blocks(int nc) {
+    return 1 + nc * FinishShape<P, Part>::kSplit;
+}
+
+// Block `blk` of the finish of one sweep (block 0: likelihood; blocks
+// 1 + (nc - 1 - I) * kSplit + h: rows h * kRows .. of row chunk I).
 template <int P, typename Part>
 __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
-    using FS = FinishShape<P>;
+    using FS = FinishShape<P, Part>;
     const Part* rowpart = static_cast<const Part*>(a.rowpart);
     const Part* colpart = static_cast<const Part*>(a.colpart);
     __shared__ double part[2][FS::kThreads];
@@ -991,8 +1014,10 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
         }
         return;
     }
-    const int I = a.nc - blk;  // the chunks with the most partials are scheduled first
-    const int g = t / FS::kOut, o = t - g * FS::kOut;  // o = r * P + q
+    const int ci = (blk - 1) / FS::kSplit;  // the chunks with the most partials are scheduled first
+    const int I = a.nc - 1 - ci;
+    const int h0 = (blk - 1 - ci * FS::kSplit) * FS::kRows;  // first row of this block within the chunk
+    const int g = t / FS::kOut, o = t - g * FS::kOut;        // o = r * P + q, row h0 + r of the chunk
     double acc = 0.0;
     if (g < FS::kGroups) {
         // row sums: units (J, I), J = 0 .. I/4, each [32 rows][P] contiguous
@@ -1003,12 +1028,12 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
             for (int k = 0; k < FS::kChunk; ++k) {
                 const int J = J0 + FS::kGroups * k;
                 const long long u = pair_units_before(J, a.nc) + (I - 4 * J);
-                v[k] = J <= j_max ? __ldcg(&rowpart[(size_t)u * FS::kOut + o]) : Part(0);
+                v[k] = J <= j_max ? __ldcg(&rowpart[(size_t)u * (kPairRows * P) + h0 * P + o]) : Part(0);
             }
             acc -= (double)tree_sum<FS::kChunk>(v);
         }
         // column sums of block J = I/4 for its rows (I % 4) * 32 + r: entries (slot, warp)
-        const int J = I >> 2, r = o / P, q = o - r * P, jj = (I & 3) * kPairRows + r;
+        const int J = I >> 2, r = o / P, q = o - r * P, jj = (I & 3) * kPairRows + h0 + r;
         const long long before = pair_units_before(J, a.nc);
         const int n_e = a.j_slots[J] * kPairWarps;
         for (int e0 = g; e0 < n_e; e0 += FS::kGroups * 8) {
@@ -1031,16 +1056,16 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
 #pragma unroll
         for (int k = 0; k < FS::kGroups; ++k) s += part[0][k * FS::kOut + t];
         grad_t = a.tau * s;
-        const int row = I * kPairRows + t / P;
-        if (row < a.n) a.grad_out[(size_t)I * FS::kOut + t] = grad_t;
+        const int row = I * kPairRows + h0 + t / P;
+        if (row < a.n) a.grad_out[(size_t)(I * kPairRows + h0) * P + t] = grad_t;
     }
     if (!a.leapfrog) return;
-    // leapfrog for the chunk's rows: thread r < 32 takes row I * 32 + r
+    // leapfrog for the block's rows: thread r < kRows takes row I * 32 + h0 + r
     __syncthreads();  // every thread has read part[0]
     if (t < FS::kOut) part[1][t] = grad_t;
     __syncthreads();
-    const int row = I * kPairRows + t;
-    if (t < kPairRows && row < a.n) {
+    const int row = I * kPairRows + h0 + t;
+    if (t < FS::kRows && row < a.n) {
         const PairLeapfrog& L = a.leap;
         const double ca = L.coef[0], cb = L.coef[1];
         double xi[P], pi[P];
@@ -1070,7 +1095,7 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
 }
 
 template <int P, typename Part>
-__global__ void __launch_bounds__(FinishShape<P>::kThreads) pair_finish_kernel(const PairArgs a) {
+__global__ void __launch_bounds__(FinishShape<P, Part>::kThreads) pair_finish_kernel(const PairArgs a) {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     pair_finish_block<P, Part>(a, (int)blockIdx.x);
 }

@@ -46,8 +46,8 @@ cudaError_t pair_launch_one(const PairMaps& maps, const PairArgs& args, cudaStre
     // the finish kernel as a programmatic dependent: launched while the sweep
     // drains, it waits in griddepcontrol.wait for the sweep's results
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)args.nc + 1);
-    cfg.blockDim = dim3(FinishShape<P>::kThreads);
+    cfg.gridDim = dim3((unsigned)pair_finish_blocks<P, typename M::Part>(args.nc));
+    cfg.blockDim = dim3(FinishShape<P, typename M::Part>::kThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
