@@ -83,6 +83,9 @@ constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_cta
 #ifndef MDSX_FINISH_CHUNK
 #define MDSX_FINISH_CHUNK 8  // row-partial loads in flight per finish thread
 #endif
+#ifndef MDSX_FINISH_COL_CHUNK
+#define MDSX_FINISH_COL_CHUNK 8  // column-partial loads in flight per finish thread
+#endif
 #ifndef MDSX_PAIR_EARLY_RELEASE
 #define MDSX_PAIR_EARLY_RELEASE 1  // FP32 packs of rows: operands to registers, stage released before the math
 #endif
@@ -959,7 +962,8 @@ struct FinishShape {
     static constexpr int kOut = kRows * P;            // outputs per block
     static constexpr int kGroups = kThreads / kOut;   // FP32: P = 1: 4, 2: 2, 3: 2, 4: 2, 5: 1, 6: 1
     static_assert(kGroups >= 1, "a finish block must hold one row chunk's outputs");
-    static constexpr int kChunk = MDSX_FINISH_CHUNK;  // loads in flight per thread
+    static constexpr int kChunk = MDSX_FINISH_CHUNK;         // row-partial loads in flight per thread
+    static constexpr int kColChunk = MDSX_FINISH_COL_CHUNK;  // column-partial loads in flight per thread
 };
 
 // Finish blocks of one sweep: the likelihood block and kSplit per row chunk.
@@ -1036,16 +1040,16 @@ __device__ __forceinline__ void pair_finish_block(const PairArgs& a, int blk) {
         const int J = I >> 2, r = o / P, q = o - r * P, jj = (I & 3) * kPairRows + h0 + r;
         const long long before = pair_units_before(J, a.nc);
         const int n_e = a.j_slots[J] * kPairWarps;
-        for (int e0 = g; e0 < n_e; e0 += FS::kGroups * 8) {
-            Part v[8];
+        for (int e0 = g; e0 < n_e; e0 += FS::kGroups * FS::kColChunk) {
+            Part v[FS::kColChunk];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < FS::kColChunk; ++k) {
                 const int e = e0 + FS::kGroups * k;  // slot e / 8, warp e % 8
                 v[k] = e < n_e ? __ldcg(&colpart[((size_t)J * a.max_slots * kPairWarps + e) * (P * kPairCols) +
                                                  q * kPairCols + jj])
                                : Part(0);
             }
-            acc += (double)tree_sum<8>(v);
+            acc += (double)tree_sum<FS::kColChunk>(v);
         }
     }
     part[0][t] = acc;
