@@ -49,6 +49,10 @@ extern "C" {
 #define MDSX_FLAG_AVX512 (1L << 9)          /* accepted and ignored */
 #define MDSX_FLAG_CUDA (1L << 10)           /* select this engine explicitly */
 #define MDSX_FLAG_DELTA_F32 (1L << 11)      /* FP64 sweep over FP32-stored delta */
+/* FP64-accurate sweep in double-float arithmetic on the FP32 pipes (not with
+ * MDSX_FLAG_FLOAT; with MDSX_FLAG_DELTA_F32 over FP32-stored delta). P <= 6,
+ * whole-matrix engines, unordered-pair schedule; not for the HMC driver. */
+#define MDSX_FLAG_DOUBLE_FLOAT (1L << 12)
 
 /* Largest embedding dimension the CUDA kernels are built for. */
 #define MDSX_MAX_DIMENSION 10

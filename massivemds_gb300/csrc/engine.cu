@@ -117,6 +117,7 @@ void free_all(mdsx_engine* e) {
     cudaFree(e->d_pair_begin);
     cudaFree(e->d_pair_jfirst);
     cudaFree(e->d_pair_jslots);
+    cudaFree(e->d_normal_table);
     if (e->h_out) cudaFreeHost(e->h_out);
     if (e->h_xstage) cudaFreeHost(e->h_xstage);
     if (e->h_grad) cudaFreeHost(e->h_grad);
@@ -130,7 +131,7 @@ void free_all(mdsx_engine* e) {
 int plan_pairs(mdsx_engine* e) {
     int ctas = 0;
     const bool f64 = !e->x_f32;
-    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, e->mode, &ctas));
+    MDSX_CUDA(e, mdsx::pair_occupancy(e->p, e->trunc, e->mode, &ctas, e->dd));
     if (ctas < 1) return fail(e, MDSX_ECUDA, "pair sweep kernel cannot be resident on this device");
     e->pair_nb = (e->n + mdsx::kPairCols - 1) / mdsx::kPairCols;
     e->pair_nc = (e->n + mdsx::kPairRows - 1) / mdsx::kPairRows;
@@ -242,8 +243,26 @@ int plan_and_allocate(mdsx_engine* e) {
         // 1.8x truncated (N = 20 000, P = 2).
         if (e->trunc || e->mode != Mode::kF32) e->schedule = MDSX_SWEEP_PAIRS;
     }
+    if (e->dd) {
+        if (e->schedule != MDSX_SWEEP_PAIRS)
+            return fail(e, MDSX_EUNSUPPORTED,
+                        "double-float pair math runs on the unordered-pair schedule only (P <= 6, whole matrix)");
+        if (e->trunc) {
+            std::vector<float> table(mdsx::kNormalDDFloats);
+            mdsx::normal_dd_table(table.data());
+            MDSX_CUDA(e, mdsx::device_malloc(&e->d_normal_table, table.size() * sizeof(float)));
+            MDSX_CUDA(e, cudaMemcpy(e->d_normal_table, table.data(), table.size() * sizeof(float),
+                                    cudaMemcpyHostToDevice));
+        }
+    }
     MDSX_CUDA(e, cudaStreamSynchronize(e->stream));
     return MDSX_OK;
+}
+
+// Caller locations (device, row-major N x P doubles) into the current SoA buffer.
+cudaError_t locations_to_soa(mdsx_engine* e, const double* d_src) {
+    return e->dd ? mdsx::convert_locations_dd(d_src, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->stream)
+                 : mdsx::convert_locations(d_src, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream);
 }
 
 // Flag row (row P) of both location buffers from the NaN-row marks.
@@ -336,6 +355,7 @@ mdsx::PairArgs make_pair_args(mdsx_engine* e) {
     pa.grad_out = a.grad_out;
     pa.sums_out = a.sums_out;
     pa.err = a.err;
+    pa.normal_table = e->d_normal_table;
     return pa;
 }
 
@@ -347,7 +367,7 @@ int enqueue_sweep(mdsx_engine* e) {
     MDSX_CUDA(e, mdsx::launch_fault());
     if (e->schedule == MDSX_SWEEP_PAIRS) {
         const mdsx::PairArgs pa = make_pair_args(e);
-        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
+        MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream, e->dd));
         e->last_launches = 2;
         return MDSX_OK;
     }
@@ -370,7 +390,7 @@ int enqueue_sweep_leapfrog(mdsx_engine* e, const mdsx::PairLeapfrog& lf) {
     mdsx::PairArgs pa = make_pair_args(e);
     pa.leapfrog = 1;
     pa.leap = lf;
-    MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream));
+    MDSX_CUDA(e, mdsx::pair_launch(e->p, e->trunc, e->mode, e->pair_maps[e->xcur], pa, e->stream, e->dd));
     e->last_launches = 2;
     return MDSX_OK;
 }
@@ -426,6 +446,8 @@ int mdsx_create_rows(int embedding_dimension, int location_count, long flags, in
     if (location_count > (1 << 20)) return fail(nullptr, MDSX_EINVAL, "locationCount above 2^20");
     if (row_begin < 0 || row_end > location_count || row_begin >= row_end)
         return fail(nullptr, MDSX_EINVAL, "row range must satisfy 0 <= row_begin < row_end <= locationCount");
+    if ((flags & MDSX_FLAG_DOUBLE_FLOAT) && (flags & MDSX_FLAG_FLOAT))
+        return fail(nullptr, MDSX_EINVAL, "MDSX_FLAG_DOUBLE_FLOAT and MDSX_FLAG_FLOAT exclude each other");
     int count = 0;
     cudaError_t err = cudaGetDeviceCount(&count);
     if (err != cudaSuccess || count == 0)
@@ -443,6 +465,7 @@ int mdsx_create_rows(int embedding_dimension, int location_count, long flags, in
     e->flags = flags;
     e->device = device;
     e->trunc = (flags & MDSX_FLAG_LEFT_TRUNCATION) != 0;
+    e->dd = (flags & MDSX_FLAG_DOUBLE_FLOAT) != 0;
     if (flags & MDSX_FLAG_FLOAT) {
         e->mode = Mode::kF32;
         e->delta_f32 = e->x_f32 = true;
@@ -524,9 +547,11 @@ int mdsx_update_locations(mdsx_engine* e, int index, const double* x, size_t len
     MDSX_CUDA(e, cudaMemcpyAsync(e->d_xin, src, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
     MDSX_CUDA(e, cudaEventRecord(e->h2d_done, e->stream));
     if (index == -1)
-        MDSX_CUDA(e, mdsx::convert_locations(e->d_xin, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+        MDSX_CUDA(e, locations_to_soa(e, e->d_xin));
     else
-        MDSX_CUDA(e, mdsx::set_one_location(e->d_xin, index, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+        MDSX_CUDA(e, e->dd ? mdsx::set_one_location_dd(e->d_xin, index, e->p, e->d_x[e->xcur], e->x_ld, e->stream)
+                           : mdsx::set_one_location(e->d_xin, index, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32,
+                                                    e->stream));
     if (!e->h_xstage) MDSX_CUDA(e, cudaEventSynchronize(e->h2d_done));
     e->sum_known = false;
     e->grad_known = false;
@@ -603,7 +628,7 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
     if (length != (size_t)e->rows * e->n)
         return fail(e, MDSX_EINVAL, "setPairwiseData: length != N*N (rows*N for a row range)");
     DeviceGuard guard(e->device);
-    if (!e->delta_f32 && e->ld == e->n) {
+    if (!e->delta_f32 && !e->dd && e->ld == e->n) {
         MDSX_CUDA(e, cudaMemcpyAsync(e->d_delta, data, length * sizeof(double), cudaMemcpyHostToDevice, e->stream));
     } else {
         // Stage rows of doubles on the device and convert/pad them in place.
@@ -616,10 +641,11 @@ int mdsx_set_pairwise_data(mdsx_engine* e, const double* data, size_t length) {
             const long long rows = std::min<long long>(rows_per_chunk, e->rows - r0);
             cudaError_t err = cudaMemcpyAsync(staging, data + r0 * e->n, (size_t)(rows * e->n) * sizeof(double),
                                               cudaMemcpyHostToDevice, e->stream);
+            void* dst = static_cast<char*>(e->d_delta) + (size_t)(r0 * e->ld) * elem;
             if (err == cudaSuccess)
-                err = mdsx::convert_delta_rows(staging, rows, e->n,
-                                               static_cast<char*>(e->d_delta) + (size_t)(r0 * e->ld) * elem, e->ld,
-                                               e->delta_f32, e->stream);
+                err = e->dd && !e->delta_f32
+                          ? mdsx::convert_delta_rows_dd(staging, rows, e->n, dst, e->ld, e->stream)
+                          : mdsx::convert_delta_rows(staging, rows, e->n, dst, e->ld, e->delta_f32, e->stream);
             if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
             if (err != cudaSuccess) {
                 cudaFree(staging);
@@ -714,7 +740,7 @@ int mdsx_update_locations_device(mdsx_engine* e, const double* d_x, size_t lengt
     if (!d_x) return fail(e, MDSX_EINVAL, "locations pointer is NULL");
     if (length != (size_t)e->n * e->p) return fail(e, MDSX_EINVAL, "length != N*P");
     DeviceGuard guard(e->device);
-    MDSX_CUDA(e, mdsx::convert_locations(d_x, e->n, e->p, e->d_x[e->xcur], e->x_ld, e->x_f32, e->stream));
+    MDSX_CUDA(e, locations_to_soa(e, d_x));
     e->sum_known = false;
     e->grad_known = false;
     return MDSX_OK;
@@ -746,6 +772,8 @@ int mdsx_set_sweep_schedule(mdsx_engine* e, int schedule) {
         return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule needs an engine over the whole matrix");
     if (schedule == MDSX_SWEEP_PAIRS && !e->d_rowpart)
         return fail(e, MDSX_EUNSUPPORTED, "the unordered-pair schedule is built for P <= 6 only");
+    if (schedule == MDSX_SWEEP_ROWS && e->dd)
+        return fail(e, MDSX_EUNSUPPORTED, "double-float pair math runs on the unordered-pair schedule only");
     if (schedule != e->schedule) {
         e->schedule = schedule;
         e->sum_known = e->grad_known = false;

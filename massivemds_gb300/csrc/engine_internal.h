@@ -25,6 +25,11 @@ struct mdsx_engine {
     bool trunc = false;
     Mode mode = Mode::kF64;
     bool delta_f32 = false, x_f32 = false;
+    // Double-float pair math (MDSX_FLAG_DOUBLE_FLOAT): storage as the FP64 mode
+    // `mode`, with FP64 delta and the locations held as (hi, lo) float pairs in
+    // their 8-byte slots; unordered-pair schedule only.
+    bool dd = false;
+    float* d_normal_table = nullptr;  // normal_dd_table, with truncation
 
     cudaStream_t own_stream = nullptr;
     cudaEvent_t h2d_done = nullptr;  // recorded after the copy of a caller's host locations

@@ -699,6 +699,7 @@ extern "C" int mdsx_hmc_run(mdsx_engine* e, const mdsx_hmc_config* cfg, const do
             return fail(e, MDSX_EINVAL, "hmc: traced location out of range");
     if (!e->data_set) return fail(e, MDSX_ESTATE, "hmc: setPairwiseData has not been called");
     if (e->rows != e->n) return fail(e, MDSX_EUNSUPPORTED, "hmc: needs an engine over the whole matrix");
+    if (e->dd) return fail(e, MDSX_EUNSUPPORTED, "hmc: not built for double-float pair math");
     if (!(e->tau > 0.0)) return fail(e, MDSX_ESTATE, "hmc: precision (setParameters) not set");
     if (cfg->learn_precision && !(cfg->precision_half_width > 0.0))
         return fail(e, MDSX_EINVAL, "hmc: precision_half_width must be > 0");

@@ -48,6 +48,8 @@
 
 #include <type_traits>
 
+#include "dd.h"
+#include "normal_dd.h"
 #include "ptx.cuh"
 #include "sweep_kernel.cuh"
 
@@ -146,6 +148,7 @@ struct PairArgs {
     int* err;
     int leapfrog;       // nonzero: the finish applies `leap` to its rows
     PairLeapfrog leap;
+    const float* normal_table;  // double-float pair math with truncation: normal_dd_table (kNormalDDFloats)
 };
 
 // Units of the column blocks before J: sum over J' < J of (nc - 4 J').
@@ -343,6 +346,7 @@ struct PairMathF32 {
     using S = float;     // delta element
     using Part = float;  // row and column partials
     static constexpr bool kXJEveryUnit = false;  // x_J is copied with the first unit of each block only
+    __device__ static void prologue(const PairArgs&) {}  // no shared tables
     // The warp copies its operands of a unit into registers and releases the
     // stage before the pair math, so the next copy into it can start a unit
     // earlier (the ring runs one more unit ahead of the consumers).
@@ -432,6 +436,7 @@ struct PairMathF32Cols {
     using Part = float;
     static constexpr int kFoldUnits = 4;  // per half: 16 r^2 terms and 8 factors of 1/Phi per unit
     static constexpr bool kXJEveryUnit = true;
+    __device__ static void prologue(const PairArgs&) {}  // no shared tables
     static constexpr bool kEarlyRelease = false;  // reads its operands from the stage during the math
     struct Cols {
         f2 acc[2][P];  // column sums of columns (l + 64 cp, l + 64 cp + 32)
@@ -574,6 +579,20 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
     }
 }
 
+// delta_ji for row 4w + r of the chunk and column j = lane + 32c of the block,
+// from B's 128-byte-swizzled boxes of 128 / sizeof(S) columns (4- or 8-byte
+// elements).
+template <typename S>
+__device__ __forceinline__ S pair_b_value(const S* sB, int lane, int warp, int c, int r) {
+    constexpr int kBoxCols = 128 / (int)sizeof(S);     // 32 (4-byte) or 16 (8-byte)
+    constexpr int kChunkElems = 16 / (int)sizeof(S);   // 4 or 2
+    const int col = 4 * warp + r;                      // column of B = row of the chunk
+    const int box = col / kBoxCols, within = col - box * kBoxCols;
+    const int jj = lane + 32 * c;                      // row of B
+    const int chunk = (within / kChunkElems) ^ (jj & 7);
+    return sB[(box * kPairCols + jj) * kBoxCols + chunk * kChunkElems + within % kChunkElems];
+}
+
 // FP64 policy: scalar FP64 pairs over FP32- or FP64-stored delta and FP64 locations;
 // FP64 partials; Phi multiplied into per-lane products, log taken every
 // kFoldUnits units.
@@ -583,6 +602,7 @@ struct PairMathF64 {
     using S = DeltaT;  // float (DELTA_F32 mode) or double (FP64 mode)
     using Part = double;
     static constexpr bool kXJEveryUnit = false;
+    __device__ static void prologue(const PairArgs&) {}  // no shared tables
     static constexpr bool kEarlyRelease = false;  // bound by the FP64 pipe: reads its operands from the stage
     static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
@@ -612,17 +632,6 @@ struct PairMathF64 {
                 cols.acc[c][q] = 0.0;
             }
     }
-    // delta_ji for row 4w + r of the chunk and column j = lane + 32c of the block,
-    // from B's 128-byte-swizzled boxes of 128 / sizeof(S) columns.
-    __device__ static S b_value(const S* sB, int lane, int warp, int c, int r) {
-        constexpr int kBoxCols = 128 / (int)sizeof(S);     // 32 (float) or 16 (double)
-        constexpr int kChunkElems = 16 / (int)sizeof(S);   // 4 or 2
-        const int col = 4 * warp + r;                      // column of B = row of the chunk
-        const int box = col / kBoxCols, within = col - box * kBoxCols;
-        const int jj = lane + 32 * c;                      // row of B
-        const int chunk = (within / kChunkElems) ^ (jj & 7);
-        return sB[(box * kPairCols + jj) * kBoxCols + chunk * kChunkElems + within % kChunkElems];
-    }
     // One unit, row by row (one row's x_i and sums live at a time).
     template <bool MASKED>
     __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
@@ -641,7 +650,7 @@ struct PairMathF64 {
             for (int c = 0; c < 4; ++c) {
                 const int j = j0 + lane + 32 * c;
                 const S a = sA[(4 * warp + r) * kPairCols + lane + 32 * c];
-                const S bb = b_value(sB, lane, warp, c, r);
+                const S bb = pair_b_value(sB, lane, warp, c, r);
                 bool vA = true, vB = true;
                 if (MASKED) {
                     const bool ok = (i < n) && (j < n) && (i > j);
@@ -669,6 +678,167 @@ struct PairMathF64 {
     __device__ static void result(Sums& s, double& r2, double& lsum) {
         r2 = s.r2;
         lsum = TRUNC ? 2.0 * (s.l2 + log(s.prod)) + s.l1 : 0.0;
+    }
+};
+
+// One unordered pair {i, j} in double-float arithmetic (pair_f64_sym's steps):
+// likelihood terms of (i, j) (delta_ij = dA) and (j, i) (delta_ji = dB), the
+// row sums of row i and the column sums of column j.
+template <int P, bool TRUNC, bool MASKED>
+__device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P], dd dA, dd dB, bool vA, bool vB,
+                                            dd sqrt_tau, dd inv_sqrt_tau, const float* tab, dd (&racc)[P],
+                                            dd (&cacc)[P], dd& r2, dd& prod, dd& prodm) {
+    dd dx[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) dx[q] = dd_sub(xi[q], xj[q]);
+    dd d2 = dd_sqr(dx[0]);
+#pragma unroll
+    for (int q = 1; q < P; ++q) d2 = dd_add(d2, dd_sqr(dx[q]));
+    if (MASKED && !(vA || vB)) return;
+    const dd rs = dd_rsqrt(d2);
+    // coincident points: d = 0 and a NaN gradient term, as in pair_f64_sym
+    const dd d = d2.hi >= 1.17549435e-38f ? dd_mul(d2, rs) : dd_of(0.0f);
+    const dd resA = dd_sub(dA, d), resB = dd_sub(dB, d);
+    if (!MASKED) {
+        r2 = dd_add(r2, dd_add(dd_sqr(resA), dd_sqr(resB)));
+    } else {
+        if (vA) r2 = dd_add(r2, dd_sqr(resA));
+        if (vB) r2 = dd_add(r2, dd_sqr(resB));
+    }
+    dd t = dd_of(0.0f);
+    if (TRUNC) {
+        const dd z = dd_mul(d, sqrt_tau);
+        dd q, pdf;
+        normal_dd(z, tab, q, pdf);
+        const dd cdf = dd_add_f(dd_neg(q), 1.0f);
+        if (MASKED) {
+            if (vA) prodm = dd_mul(prodm, cdf);
+            if (vB) prodm = dd_mul(prodm, cdf);
+        } else {
+            prod = dd_mul(prod, cdf);
+        }
+        t = dd_mul(dd_mul(pdf, rs), dd_mul(dd_rcp(cdf), inv_sqrt_tau));
+    }
+    if (!MASKED || vA) {
+        const dd nc = dd_sub(t, dd_mul(resA, rs));
+#pragma unroll
+        for (int q = 0; q < P; ++q) racc[q] = dd_fma(nc, dx[q], racc[q]);
+    }
+    if (!MASKED || vB) {
+        const dd nc = dd_sub(t, dd_mul(resB, rs));
+#pragma unroll
+        for (int q = 0; q < P; ++q) cacc[q] = dd_fma(nc, dx[q], cacc[q]);
+    }
+}
+
+// Double-float policy: the FP64 modes' accuracy from the FP32 pipes. Locations
+// arrive as (hi, lo) float pairs in 8-byte slots; delta as FP32 (DeltaT =
+// float) or as (hi, lo) pairs in 8-byte slots (DeltaT = double). FP64 partials,
+// as the FP64 policy. With truncation each CTA copies the normal tail table
+// into shared memory first.
+template <int P, bool TRUNC, typename DeltaT>
+struct PairMathDD {
+    using X = double;
+    using S = DeltaT;
+    using Part = double;
+    static constexpr bool kXJEveryUnit = false;
+    static constexpr bool kEarlyRelease = false;
+    // 16 factors >= 1/2 per unit on the fast path: >= 2^-64 per fold, well inside FP32's range
+    static constexpr int kFoldUnits = 4;
+    struct Cols {
+        dd xj[4][P];
+        dd acc[4][P];
+    };
+    struct Sums {
+        dd r2, prod;
+        double l2, l1;  // as PairMathF64
+        int since_fold;
+    };
+    dd sqrt_tau, inv_sqrt_tau;
+
+    __device__ explicit PairMathDD(const PairArgs& a)
+        : sqrt_tau(dd_from_double(a.sqrt_tau)), inv_sqrt_tau(dd_from_double(1.0 / a.sqrt_tau)) {}
+
+    __device__ static float* table() {
+        __shared__ __align__(16) float tab[TRUNC ? kNormalDDFloats : 4];
+        return tab;
+    }
+    // Every thread of the CTA takes part; the kernel synchronises after it.
+    __device__ static void prologue(const PairArgs& a) {
+        if (!TRUNC) return;
+        const float4* src = reinterpret_cast<const float4*>(a.normal_table);
+        float4* dst = reinterpret_cast<float4*>(table());
+        for (int k = threadIdx.x; k < kNormalDDFloats / 4; k += blockDim.x) dst[k] = __ldg(&src[k]);
+    }
+    // an 8-byte slot holding (hi, lo) as two floats, low word first
+    __device__ static dd slot(double v) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+        return dd_of(__int_as_float((int)(unsigned)(b & 0xffffffffull)), __int_as_float((int)(unsigned)(b >> 32)));
+    }
+    __device__ static dd delta(float v) { return dd_of(v); }
+    __device__ static dd delta(double v) { return slot(v); }
+
+    __device__ static void init(Sums& s) {
+        s.r2 = dd_of(0.0f);
+        s.prod = dd_of(1.0f);
+        s.l2 = s.l1 = 0.0;
+        s.since_fold = 0;
+    }
+    __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                cols.xj[c][q] = slot(sXJ[q * kPairCols + lane + 32 * c]);
+                cols.acc[c][q] = dd_of(0.0f);
+            }
+    }
+    template <bool MASKED>
+    __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
+                         int lane, int warp, Part (&v)[4 * P]) const {
+        const float* tab = table();
+        dd prodm = dd_of(1.0f);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            dd xi[P], racc[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                xi[q] = slot(sXI[q * kPairRows + 4 * warp + r]);
+                racc[q] = dd_of(0.0f);
+            }
+            const int i = i0 + r;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int j = j0 + lane + 32 * c;
+                const dd a = delta(sA[(4 * warp + r) * kPairCols + lane + 32 * c]);
+                const dd bb = delta(pair_b_value(sB, lane, warp, c, r));
+                bool vA = true, vB = true;
+                if (MASKED) {
+                    const bool ok = (i < n) && (j < n) && (i > j);
+                    vA = ok && (a.hi == a.hi);
+                    vB = ok && (bb.hi == bb.hi);
+                }
+                pair_dd_sym<P, TRUNC, MASKED>(xi, cols.xj[c], a, bb, vA, vB, sqrt_tau, inv_sqrt_tau, tab, racc,
+                                              cols.acc[c], s.r2, s.prod, prodm);
+            }
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[r * P + q] = dd_to_double(racc[q]);
+        }
+        if (MASKED && TRUNC) s.l1 += log(dd_to_double(prodm));  // <= 32 factors >= 1/2
+    }
+    __device__ static void after_unit(Sums& s) {
+        if (++s.since_fold == kFoldUnits) {
+            s.since_fold = 0;
+            if (TRUNC) {
+                s.l2 += log(dd_to_double(s.prod));
+                s.prod = dd_of(1.0f);
+            }
+        }
+    }
+    __device__ static Part col_value(const Cols& cols, int c, int q) { return dd_to_double(cols.acc[c][q]); }
+    __device__ static void result(Sums& s, double& r2, double& lsum) {
+        r2 = dd_to_double(s.r2);
+        lsum = TRUNC ? 2.0 * (s.l2 + log(dd_to_double(s.prod))) + s.l1 : 0.0;
     }
 };
 
@@ -827,6 +997,7 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
         prefetch_tensormap(&tmap_xi);
         prefetch_tensormap(&tmap_xj);
     }
+    M::prologue(a);
     __syncthreads();
 
     // Copy issue state (thread 0 only): next unit to issue and its (J, I).

@@ -9,6 +9,26 @@
 namespace mdsx {
 namespace {
 
+// An 8-byte slot holding a double as the double-float pair (hi, lo), low word
+// first: the location and delta layout of the double-float pair math. A NaN is
+// stored as a float NaN in hi and 0x7ff80000 in lo, which is a NaN both as a
+// float and as the high word of a double, so the slot reads as NaN to the pair
+// math (hi) and to the FP64 NaN-row scan (mark_nan_rows) alike.
+struct DDSlot {
+    float hi, lo;
+    DDSlot() = default;
+    __device__ explicit DDSlot(double v) {
+        if (isnan(v)) {
+            hi = __int_as_float(0x7fc00000);
+            lo = __int_as_float(0x7ff80000);
+            return;
+        }
+        hi = (float)v;
+        lo = isfinite(hi) ? (float)(v - (double)hi) : 0.0f;
+    }
+};
+static_assert(sizeof(DDSlot) == 8, "a double-float slot is 8 bytes");
+
 template <typename C>
 __global__ void convert_locations_kernel(const double* __restrict__ src, int n, int p, C* __restrict__ dst, int x_ld) {
     const long long total = (long long)p * x_ld;
@@ -104,6 +124,23 @@ cudaError_t set_one_location(const double* src, int index, int p, void* dst, int
         set_one_location_kernel<float><<<1, 32, 0, s>>>(src, index, p, static_cast<float*>(dst), x_ld);
     else
         set_one_location_kernel<double><<<1, 32, 0, s>>>(src, index, p, static_cast<double*>(dst), x_ld);
+    return cudaGetLastError();
+}
+
+cudaError_t convert_locations_dd(const double* src, int n, int p, void* dst, int x_ld, cudaStream_t s) {
+    const int grid = grid_for((long long)p * x_ld, 256);
+    convert_locations_kernel<DDSlot><<<grid, 256, 0, s>>>(src, n, p, static_cast<DDSlot*>(dst), x_ld);
+    return cudaGetLastError();
+}
+
+cudaError_t set_one_location_dd(const double* src, int index, int p, void* dst, int x_ld, cudaStream_t s) {
+    set_one_location_kernel<DDSlot><<<1, 32, 0, s>>>(src, index, p, static_cast<DDSlot*>(dst), x_ld);
+    return cudaGetLastError();
+}
+
+cudaError_t convert_delta_rows_dd(const double* src, long long rows, int n, void* dst, long long ld, cudaStream_t s) {
+    convert_delta_rows_kernel<DDSlot><<<grid_for(rows * n, 256), 256, 0, s>>>(src, rows, n, static_cast<DDSlot*>(dst),
+                                                                              ld);
     return cudaGetLastError();
 }
 

@@ -425,6 +425,7 @@ int mdsx_surrogate_create(mdsx_engine* e, int landmarks, int hidden_width, int h
     if (max_rows < 64) return fail(e, MDSX_EINVAL, "surrogate: max_rows must be >= 64");
     if (!e->data_set) return fail(e, MDSX_ESTATE, "surrogate: setPairwiseData has not been called");
     if (e->rows != e->n) return fail(e, MDSX_EUNSUPPORTED, "surrogate: needs an engine over the whole matrix");
+    if (e->dd) return fail(e, MDSX_EUNSUPPORTED, "surrogate: not built for double-float pair math");
     mdsx::internal::DeviceGuard guard(e->device);
     auto* s = new mdsx_surrogate;
     s->engine = e;

@@ -57,10 +57,16 @@ struct PairMaps {
 };
 // Built for every precision mode with P <= kPairMaxP.
 bool pair_built(Mode mode, int p);
-cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm);
+// dd: double-float pair math over the FP64 modes' storage (mode kF64DeltaF32:
+// FP32 delta; kF64: delta and locations as (hi, lo) float pairs in 8-byte slots).
+cudaError_t pair_occupancy(int p, bool trunc, Mode mode, int* ctas_per_sm, bool dd = false);
 // Enqueues the pair sweep and its finish kernel (two launches).
 cudaError_t pair_launch(int p, bool trunc, Mode mode, const PairMaps& maps, const PairArgs& args,
-                        cudaStream_t stream);
+                        cudaStream_t stream, bool dd = false);
+// The double-float instances (sweep_pairs_dd.cu), P <= kPairMaxP64.
+cudaError_t pair_occupancy_dd(int p, bool trunc, bool delta_f32, int* ctas_per_sm);
+cudaError_t pair_launch_dd(int p, bool trunc, bool delta_f32, const PairMaps& maps, const PairArgs& args,
+                           cudaStream_t stream);
 // flags[j] = 1 for j >= n or a NaN in row j of delta (row_nan), else 0, for j < x_ld,
 // in the location type (float or double).
 cudaError_t write_flag_row(const int* row_nan, int n, int rows_padded, void* flags, bool is_f32, int x_ld,
@@ -76,6 +82,11 @@ cudaError_t convert_locations(const double* src, int n, int p, void* dst, int x_
 cudaError_t set_one_location(const double* src, int index, int p, void* dst, int x_ld, bool to_f32, cudaStream_t s);
 // rows [row0, row0+rows) of a row-major double matrix with n columns -> rows of a
 // matrix with leading dimension ld in float (NaN kept) or double.
+// The double-float layout: each double as (hi, lo) floats in its 8-byte slot
+// (NaN in both words), for the double-float pair math.
+cudaError_t convert_locations_dd(const double* src, int n, int p, void* dst, int x_ld, cudaStream_t s);
+cudaError_t set_one_location_dd(const double* src, int index, int p, void* dst, int x_ld, cudaStream_t s);
+cudaError_t convert_delta_rows_dd(const double* src, long long rows, int n, void* dst, long long ld, cudaStream_t s);
 cudaError_t convert_delta_rows(const double* src, long long rows, int n, void* dst, long long ld, bool to_f32,
                                cudaStream_t s);
 // Same from float rows into float storage.

@@ -14,6 +14,7 @@ AVX = 1 << 8
 AVX512 = 1 << 9
 CUDA = 1 << 10
 DELTA_F32 = 1 << 11
+DOUBLE_FLOAT = 1 << 12  # FP64-accurate double-float pair math on the FP32 pipes (P <= 6)
 
 MAX_DIMENSION = 10
 

@@ -1,0 +1,70 @@
+// Host check of the double-float arithmetic (massivemds_gb300/csrc/dd.h) and the
+// double-float normal tail table (normal_dd.h) against long double references.
+// Prints one line per check: name, max error, bound; exits 1 if a bound fails.
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+#include "dd.h"
+#include "normal_dd.h"
+
+using namespace mdsx;
+
+static int failures = 0;
+
+static void report(const char* name, long double err, long double bound) {
+    std::printf("%s %.3Le %.1Le\n", name, err, bound);
+    if (!(err <= bound)) ++failures;
+}
+
+static long double ld(dd a) { return (long double)a.hi + (long double)a.lo; }
+
+int main() {
+    std::mt19937_64 rng(12345);
+    std::uniform_real_distribution<double> uni(-4.0, 4.0);
+    long double e_add = 0, e_mul = 0, e_sqr = 0, e_fma = 0, e_rsq = 0, e_rcp = 0, e_split = 0;
+    for (int t = 0; t < 200000; ++t) {
+        const double x = uni(rng), y = uni(rng), w = uni(rng);
+        const dd a = dd_from_double(x), b = dd_from_double(y), c = dd_from_double(w);
+        const long double A = ld(a), B = ld(b), C = ld(c);
+        e_split = std::max(e_split, std::fabs(A - (long double)x) / std::fabs((long double)x));
+        if (std::fabs(A + B) > 1e-3L) e_add = std::max(e_add, std::fabs(ld(dd_add(a, b)) - (A + B)) / (std::fabs(A) + std::fabs(B)));
+        e_mul = std::max(e_mul, std::fabs(ld(dd_mul(a, b)) - A * B) / std::fabs(A * B));
+        e_sqr = std::max(e_sqr, std::fabs(ld(dd_sqr(a)) - A * A) / (A * A));
+        const long double f = C + A * B;
+        e_fma = std::max(e_fma, std::fabs(ld(dd_fma(a, b, c)) - f) / (std::fabs(C) + std::fabs(A * B)));
+        const long double ax = std::fabs(A) + 1e-3L;
+        const dd pa = dd_from_double((double)ax);
+        e_rsq = std::max(e_rsq, std::fabs(ld(dd_rsqrt(pa)) * std::sqrt(ld(pa)) - 1.0L));
+        e_rcp = std::max(e_rcp, std::fabs(ld(dd_rcp(a)) * A - 1.0L));
+    }
+    report("split", e_split, 1e-14L);
+    report("add", e_add, 2e-14L);
+    report("mul", e_mul, 2e-14L);
+    report("sqr", e_sqr, 2e-14L);
+    report("fma", e_fma, 2e-14L);
+    report("rsqrt", e_rsq, 1e-13L);
+    report("rcp", e_rcp, 1e-13L);
+
+    static float tab[kNormalDDFloats];
+    normal_dd_table(tab);
+    const long double inv_sqrt_2pi = 0.398942280401432677939946059934381868L;
+    long double e_q = 0, e_phi = 0, e_q_rel = 0;
+    std::uniform_real_distribution<double> zd(0.0, 9.0);
+    for (int t = 0; t < 400000; ++t) {
+        const double zz = t < 1000 ? t * (9.0 / 1000) : zd(rng);
+        const dd z = dd_from_double(zz);
+        const long double Z = ld(z);
+        dd q, phi;
+        normal_dd(z, tab, q, phi);
+        const long double Q = 0.5L * std::erfc(Z / std::sqrt(2.0L));
+        const long double PHI = inv_sqrt_2pi * std::exp(-0.5L * Z * Z);
+        e_q = std::max(e_q, std::fabs(ld(q) - Q));
+        e_phi = std::max(e_phi, std::fabs(ld(phi) - PHI));
+        if (Z < 8.0L) e_q_rel = std::max(e_q_rel, std::fabs(ld(q) - Q) / Q);
+    }
+    report("normal_Q_abs", e_q, 5e-14L);
+    report("normal_Q_rel_z<8", e_q_rel, 5e-10L);
+    report("normal_phi_abs", e_phi, 5e-14L);
+    return failures ? 1 : 0;
+}

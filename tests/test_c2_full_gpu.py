@@ -10,12 +10,14 @@ mirrored and clipped at 0, stored FP32 (1.6 GB) -- the matrix bench.py times.
   src/NewMultiDimensionalScaling.hpp:193-334). Every precision mode and both
   sweep schedules are compared with the double engine: FP64 pair arithmetic
   over FP32-stored delta and over FP64-stored delta within 1e-10 (sum) and
-  1e-9 (gradient, max |dg| / max |g|), the FP32 mode within 1e-5; the FP32
+  1e-9 (gradient, max |dg| / max |g|), and so are the double-float modes
+  ("dd32" over FP32-stored delta, "dd" over FP64-stored delta); the FP32 mode
+  within 1e-5; the FP32
   mode must also land closer to the double engine than the reference's own
   FLOAT engine does.
 * Oracle: twenty more states at fresh locations, each evaluated by the FP64
-  oracle (threaded, compensated) and by the FP32, FP64-over-FP32 and
-  FP64-stored engines, with the same tolerances.
+  oracle (threaded, compensated) and by the FP32, FP64-over-FP32,
+  FP64-stored and double-float-over-FP32 engines, with the same tolerances.
 
 delta is regenerated from its seed and checked against the fingerprint stored
 with the golden vectors before anything is compared.
@@ -46,6 +48,8 @@ MODES = {  # name: (flags, delta stored as FP64?, schedule or None for the defau
     "f64s32rows": (F.DELTA_F32, False, F.SWEEP_ROWS),
     "f64": (0, True, None),
     "f64rows": (0, True, F.SWEEP_ROWS),
+    "dd32": (F.DOUBLE_FLOAT | F.DELTA_F32, False, None),
+    "dd": (F.DOUBLE_FLOAT, True, None),
 }
 
 
@@ -107,7 +111,7 @@ def test_full_size_against_reference_engine(c2, mode):
 
 def test_full_size_fresh_states_against_oracle(c2):
     delta, _ = c2
-    engines = {m: make_engine(m, delta) for m in ("f32", "f64s32", "f64")}
+    engines = {m: make_engine(m, delta) for m in ("f32", "f64s32", "f64", "dd32")}
     rng = np.random.default_rng(20001)
     try:
         for k in range(FRESH_STATES):
