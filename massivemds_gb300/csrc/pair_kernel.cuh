@@ -799,6 +799,12 @@ struct PairMathDD {
         const float* tab = table();
         dd prodm = dd_of(1.0f);
 #pragma unroll
+        for (int k = 0; k < 4 * P; ++k) v[k] = 0.0;
+        // Rows one at a time in a loop that is not unrolled (the four column
+        // slots are): an unrolled unit is ~16 x 450 instructions and misses in
+        // the instruction cache. The row sums rotate through v, so that every
+        // register index stays a constant.
+#pragma unroll 1
         for (int r = 0; r < 4; ++r) {
             dd xi[P], racc[P];
 #pragma unroll
@@ -822,7 +828,9 @@ struct PairMathDD {
                                               cols.acc[c], s.r2, s.prod, prodm);
             }
 #pragma unroll
-            for (int q = 0; q < P; ++q) v[r * P + q] = dd_to_double(racc[q]);
+            for (int k = 0; k < 3 * P; ++k) v[k] = v[k + P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) v[3 * P + q] = dd_to_double(racc[q]);
         }
         if (MASKED && TRUNC) s.l1 += log(dd_to_double(prodm));  // <= 32 factors >= 1/2
     }
