@@ -347,6 +347,7 @@ struct PairMathF32 {
     using Part = float;  // row and column partials
     static constexpr bool kXJEveryUnit = false;  // x_J is copied with the first unit of each block only
     __device__ static void prologue(const PairArgs&) {}  // no shared tables
+    static constexpr int kMinCtas = 0;  // pair_min_ctas_of decides
     // The warp copies its operands of a unit into registers and releases the
     // stage before the pair math, so the next copy into it can start a unit
     // earlier (the ring runs one more unit ahead of the consumers).
@@ -437,6 +438,7 @@ struct PairMathF32Cols {
     static constexpr int kFoldUnits = 4;  // per half: 16 r^2 terms and 8 factors of 1/Phi per unit
     static constexpr bool kXJEveryUnit = true;
     __device__ static void prologue(const PairArgs&) {}  // no shared tables
+    static constexpr int kMinCtas = 0;  // pair_min_ctas_of decides
     static constexpr bool kEarlyRelease = false;  // reads its operands from the stage during the math
     struct Cols {
         f2 acc[2][P];  // column sums of columns (l + 64 cp, l + 64 cp + 32)
@@ -603,6 +605,7 @@ struct PairMathF64 {
     using Part = double;
     static constexpr bool kXJEveryUnit = false;
     __device__ static void prologue(const PairArgs&) {}  // no shared tables
+    static constexpr int kMinCtas = 0;  // pair_min_ctas_of decides
     static constexpr bool kEarlyRelease = false;  // bound by the FP64 pipe: reads its operands from the stage
     static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
@@ -743,6 +746,12 @@ struct PairMathDD {
     using Part = double;
     static constexpr bool kXJEveryUnit = false;
     static constexpr bool kEarlyRelease = false;
+#ifndef MDSX_DD_TWO_CTAS_MAX_P
+#define MDSX_DD_TWO_CTAS_MAX_P 2  // compiled for two CTAs per SM (128 registers, no spills) up to this P
+#endif
+    // two CTAs per SM where 128 registers hold the unit without spills; the
+    // occupancy query then also counts shared memory (FP64-stored delta: one)
+    static constexpr int kMinCtas = P <= MDSX_DD_TWO_CTAS_MAX_P ? 2 : 1;
     // 16 factors >= 1/2 per unit on the fast path: >= 2^-64 per fold, well inside FP32's range
     static constexpr int kFoldUnits = 4;
     struct Cols {
@@ -968,7 +977,7 @@ constexpr int pair_min_ctas() {
 // spill 400-700 bytes (same time at N = 1000 and 20 000, one CTA slightly ahead).
 template <int P, class M>
 constexpr int pair_min_ctas_of() {
-    return std::is_same<typename M::Part, double>::value ? 1 : pair_min_ctas<P>();
+    return M::kMinCtas > 0 ? M::kMinCtas : std::is_same<typename M::Part, double>::value ? 1 : pair_min_ctas<P>();
 }
 
 template <int P, bool TRUNC, class M>
