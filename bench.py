@@ -350,7 +350,22 @@ def measure_c1(local, steps, warmup):
     n, p, tau, iters = 1000, 2, 1.0, 100
     delta = gen.euclidean_delta(n, dim=10, seed=666)
     xs = np.random.default_rng(667).standard_normal((warmup + steps, iters, n, p))
-    e = m.Engine(p, n, m.flags.LEFT_TRUNCATION, local)
+    line = c1_run(local, m.flags.LEFT_TRUNCATION, delta, xs, n, p, tau, iters, steps, warmup)
+    dd = c1_run(local, m.flags.LEFT_TRUNCATION | m.flags.DOUBLE_FLOAT, delta, xs, n, p, tau, iters, steps, warmup,
+                baseline=False)
+    line["double_float"] = {k: dd[k] for k in ("value", "unit", "ms_per_step", "parity", "clocks")}
+    line["double_float"]["arithmetic"] = "double-float (f32 pairs) at the FP64 bars"
+    return line
+
+
+def c1_run(local, flags, delta, xs, n, p, tau, iters, steps, warmup, baseline=True):
+    """C1 with the given engine flags (FP64 or double-float pair math); with
+    `baseline`, also the oracle port's CPU timing."""
+    import numpy as np
+
+    import massivemds_gb300 as m
+
+    e = m.Engine(p, n, flags, local)
     e.setPairwiseData(delta)
     e.setParameters([tau])
     grad = np.empty(n * p)
@@ -383,7 +398,7 @@ def measure_c1(local, steps, warmup):
     ll_ref = oracle.log_likelihood(s_ref, n, tau)
     cores = os.cpu_count() or 1
     base = {}
-    for label, threads in (("threaded_f64", cores), ("serial_f64", 1)):
+    for label, threads in (("threaded_f64", cores), ("serial_f64", 1)) if baseline else ():
         t = time.perf_counter()
         sample_iters = 10
         for k in range(sample_iters):
@@ -404,7 +419,7 @@ def measure_c1(local, steps, warmup):
                    "grad_rel": grad_rel(grad, g_ref), "iterations_checked": 1,
                    "tolerance": [PARITY_TOL["f64_sum"], PARITY_TOL["f64_grad"]]},
         "clocks": clocks,
-        "cpu_baseline": dict(base["threaded_f64"], kind="port", paths=base),
+        "cpu_baseline": dict(base["threaded_f64"], kind="port", paths=base) if baseline else None,
     }
 
 
@@ -585,16 +600,18 @@ def measure_noalloc(local, delta, xs, refs, calls=20, warmup=3):
                        "tolerance": PARITY_TOL["f32"]}}
 
 
-def measure_f64(local, delta, xs, refs, steps=10, warmup=3):
-    """FP64 pair arithmetic over the FP32-stored delta (DELTA_F32): evals/s and
-    the sweep's kernel time; the FP64 results at the checked states against
-    the oracle."""
+def measure_f64(local, delta, xs, refs, steps=10, warmup=3, double_float=False):
+    """FP64-accurate pair arithmetic over the FP32-stored delta (DELTA_F32):
+    evals/s and the sweep's kernel time; the results at the checked states
+    against the oracle at the FP64 bars. double_float: the double-float pair
+    math on the FP32 pipes (MDSX_FLAG_DOUBLE_FLOAT) instead of FP64."""
     import torch
 
     import massivemds_gb300 as m
 
     n = delta.shape[0]
-    eng = m.Engine(P, n, m.flags.DELTA_F32 | m.flags.LEFT_TRUNCATION, local)
+    flags = m.flags.DELTA_F32 | m.flags.LEFT_TRUNCATION | (m.flags.DOUBLE_FLOAT if double_float else 0)
+    eng = m.Engine(P, n, flags, local)
     eng.setPairwiseData(delta)
     eng.setParameters([TAU])
     stream = torch.cuda.Stream()
@@ -630,9 +647,11 @@ def measure_f64(local, delta, xs, refs, steps=10, warmup=3):
     eng.close()
     hbm_peak, _ = peaks()
     gbs = (float(n) * n * 4 + 2.0 * n * P * 8) / (kernel_ms / 1e3) / 1e9
+    kernel = ("pair_kernel<2,true,PairMathDD<float>> + pair_finish_kernel<2,double>" if double_float
+              else "pair_kernel<2,true,PairMathF64<float>> + pair_finish_kernel<2,double>")
     return {"value": steps / (elapsed_ms / 1e3), "unit": UNIT, "steps": steps, "kernel_ms": kernel_ms,
-            "kernel": "pair_kernel<2,true,PairMathF64<float>> + pair_finish_kernel<2,double>",
-            "hbm_gbs": gbs, "hbm_frac": gbs / hbm_peak, "bound": "FP64 pipe",
+            "kernel": kernel, "arithmetic": "double-float (f32 pairs)" if double_float else "f64",
+            "hbm_gbs": gbs, "hbm_frac": gbs / hbm_peak, "bound": "FP32 pipes" if double_float else "FP64 pipe",
             "parity": {"sum_rel_max": worst_s, "grad_rel_max": worst_g, "evals_checked": len(xs),
                        "tolerance": [PARITY_TOL["f64_sum"], PARITY_TOL["f64_grad"]]},
             "clocks": clocks}
@@ -908,6 +927,8 @@ def run_mdsx(args):
                     "sums_finite": int(np.isfinite(timed_sums).sum()), "tolerance": [tol_s, tol_g]}
             if "f64" in sections and not f64:
                 line["f64"] = measure_f64(local, delta, xs, refs)
+                # the same FP64 bars from the FP32 pipes
+                line["f64"]["double_float"] = measure_f64(local, delta, xs, refs, double_float=True)
             if "noalloc" in sections and not f64 and n <= 32768:
                 line["noalloc"] = measure_noalloc(local, delta, xs, refs)
         del delta
