@@ -693,21 +693,18 @@ __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P]
                                             dd (&cacc)[P], dd& r2, dd& prod, dd& prodm) {
     dd dx[P];
 #pragma unroll
-    for (int q = 0; q < P; ++q) dx[q] = dd_sub(xi[q], xj[q]);
-    dd d2 = dd_sqr(dx[0]);
+    for (int q = 0; q < P; ++q) dx[q] = dd_sub(xi[q], xj[q]);  // normalised: products drop lo * lo
+    dd d2 = dd_of(0.0f);
 #pragma unroll
-    for (int q = 1; q < P; ++q) d2 = dd_add(d2, dd_sqr(dx[q]));
+    for (int q = 0; q < P; ++q) dd_acc_sqr(d2, dx[q]);
+    d2 = fast_two_sum(d2.hi, d2.lo);
     if (MASKED && !(vA || vB)) return;
     const dd rs = dd_rsqrt(d2);
     // coincident points: d = 0 and a NaN gradient term, as in pair_f64_sym
     const dd d = d2.hi >= 1.17549435e-38f ? dd_mul(d2, rs) : dd_of(0.0f);
     const dd resA = dd_sub(dA, d), resB = dd_sub(dB, d);
-    if (!MASKED) {
-        r2 = dd_add(r2, dd_add(dd_sqr(resA), dd_sqr(resB)));
-    } else {
-        if (vA) r2 = dd_add(r2, dd_sqr(resA));
-        if (vB) r2 = dd_add(r2, dd_sqr(resB));
-    }
+    if (!MASKED || vA) dd_acc_sqr(r2, resA);
+    if (!MASKED || vB) dd_acc_sqr(r2, resB);
     dd t = dd_of(0.0f);
     if (TRUNC) {
         const dd z = dd_mul(d, sqrt_tau);
@@ -725,12 +722,12 @@ __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P]
     if (!MASKED || vA) {
         const dd nc = dd_sub(t, dd_mul(resA, rs));
 #pragma unroll
-        for (int q = 0; q < P; ++q) racc[q] = dd_fma(nc, dx[q], racc[q]);
+        for (int q = 0; q < P; ++q) dd_acc_fma(racc[q], nc, dx[q]);
     }
     if (!MASKED || vB) {
         const dd nc = dd_sub(t, dd_mul(resB, rs));
 #pragma unroll
-        for (int q = 0; q < P; ++q) cacc[q] = dd_fma(nc, dx[q], cacc[q]);
+        for (int q = 0; q < P; ++q) dd_acc_fma(cacc[q], nc, dx[q]);
     }
 }
 
@@ -841,6 +838,12 @@ struct PairMathDD {
 #pragma unroll
             for (int q = 0; q < P; ++q) v[3 * P + q] = dd_to_double(racc[q]);
         }
+        // the long-lived accumulators: renormalised once per unit (dd_acc_fma)
+        s.r2 = dd_renorm(s.r2);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int q = 0; q < P; ++q) cols.acc[c][q] = dd_renorm(cols.acc[c][q]);
         if (MASKED && TRUNC) s.l1 += log(dd_to_double(prodm));  // <= 32 factors >= 1/2
     }
     __device__ static void after_unit(Sums& s) {

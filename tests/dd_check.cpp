@@ -38,6 +38,29 @@ int main() {
         e_rsq = std::max(e_rsq, std::fabs(ld(dd_rsqrt(pa)) * std::sqrt(ld(pa)) - 1.0L));
         e_rcp = std::max(e_rcp, std::fabs(ld(dd_rcp(a)) * A - 1.0L));
     }
+    // accumulators: 20 000 products of mixed sign (a row's gradient sum) and
+    // squares (the likelihood's sum), against long double, relative to sum |terms|
+    long double e_dot = 0, e_sq = 0;
+    for (int rep = 0; rep < 20; ++rep) {
+        dd acc = dd_of(0.0f), sq = dd_of(0.0f);
+        long double ref = 0, ref_abs = 0, ref_sq = 0;
+        for (int t = 0; t < 20000; ++t) {
+            const dd a = dd_from_double(uni(rng)), b = dd_from_double(uni(rng));
+            dd_acc_fma(acc, a, b);
+            dd_acc_sqr(sq, a);
+            if (t % 32 == 31) {  // as the pair kernel: once per unit
+                acc = dd_renorm(acc);
+                sq = dd_renorm(sq);
+            }
+            ref += ld(a) * ld(b);
+            ref_abs += std::fabs(ld(a) * ld(b));
+            ref_sq += ld(a) * ld(a);
+        }
+        e_dot = std::max(e_dot, std::fabs((long double)dd_to_double(acc) - ref) / ref_abs);
+        e_sq = std::max(e_sq, std::fabs((long double)dd_to_double(sq) - ref_sq) / ref_sq);
+    }
+    report("acc_fma_20000", e_dot, 1e-12L);
+    report("acc_sqr_20000", e_sq, 1e-12L);
     report("split", e_split, 1e-14L);
     report("add", e_add, 2e-14L);
     report("mul", e_mul, 2e-14L);
