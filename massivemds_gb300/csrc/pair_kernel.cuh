@@ -744,11 +744,13 @@ struct PairMathDD {
     static constexpr bool kXJEveryUnit = false;
     static constexpr bool kEarlyRelease = false;
 #ifndef MDSX_DD_TWO_CTAS_MAX_P
-#define MDSX_DD_TWO_CTAS_MAX_P 2  // compiled for two CTAs per SM (128 registers, no spills) up to this P
+#define MDSX_DD_TWO_CTAS_MAX_P 3  // FP32-stored delta: compiled for two CTAs per SM up to this P
 #endif
-    // two CTAs per SM where 128 registers hold the unit without spills; the
-    // occupancy query then also counts shared memory (FP64-stored delta: one)
-    static constexpr int kMinCtas = P <= MDSX_DD_TWO_CTAS_MAX_P ? 2 : 1;
+    // Two CTAs per SM (128 registers) over FP32-stored delta, where two fit in
+    // shared memory; measured on GB300: P = 2 3.72 -> 3.04 ms (no spills), P = 3
+    // 4.28 -> 3.95 ms (200 bytes spilled) at N = 20 000. FP64-stored delta fits
+    // one CTA per SM, which keeps up to 255 registers (P = 3 at 128: +21 %).
+    static constexpr int kMinCtas = sizeof(DeltaT) == 4 && P <= MDSX_DD_TWO_CTAS_MAX_P ? 2 : 1;
     // 16 factors >= 1/2 per unit on the fast path: >= 2^-64 per fold, well inside FP32's range
     static constexpr int kFoldUnits = 4;
     struct Cols {
