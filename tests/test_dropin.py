@@ -3,9 +3,9 @@ compiled program: tests/dropin_driver.cpp builds the engine through a
 factory-shaped function and replays the reference benchmark's call sequence
 (src/benchmark.cpp:167-309) on the golden sequence data, which the reference
 engine itself produced (tests/golden/make_golden.py). The CPU test compiles and
-links the driver; the GPU test runs it in FP64 (1e-10 sum, 1e-9 gradient) and
-FP32 (1e-5) and also has it check the interface's protected flags and its
-exception on a wrong length."""
+links the driver; the GPU test runs it in FP64 and in double-float (both at 1e-10
+sum, 1e-9 gradient) and FP32 (1e-5) and also has it check the interface's
+protected flags and its exception on a wrong length."""
 import os
 import shutil
 import subprocess
@@ -15,7 +15,7 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(REPO, "tests", "dropin_driver.cpp")
-FLAG_FLOAT, FLAG_OPENCL, FLAG_TRUNC = 1 << 2, 1 << 4, 1 << 5
+FLAG_FLOAT, FLAG_OPENCL, FLAG_TRUNC, FLAG_DOUBLE_FLOAT = 1 << 2, 1 << 4, 1 << 5, 1 << 12
 
 
 def _build(mdsx_lib, out_dir):
@@ -38,6 +38,7 @@ def test_dropin_driver_builds_and_links(mdsx_lib, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("flags,tol_s,tol_g", [(FLAG_OPENCL | FLAG_TRUNC, 1e-10, 1e-9),
+                                               (FLAG_OPENCL | FLAG_TRUNC | FLAG_DOUBLE_FLOAT, 1e-10, 1e-9),
                                                (FLAG_OPENCL | FLAG_TRUNC | FLAG_FLOAT, 1e-5, 1e-5)])
 def test_dropin_replays_the_reference_benchmark_sequence(mdsx_lib, golden, tmp_path, flags, tol_s, tol_g):
     data, _ = golden
