@@ -158,6 +158,16 @@ __host__ __device__ __forceinline__ dd dd_rsqrt(dd a) {
     return fast_two_sum(r0, r0 * (0.5f * e));
 }
 
+// a / b for b != 0: q1 = a_hi / b_hi from the FP32 seed, the remainder
+// a - q1 b in double-float, and one correction q2 = remainder / b_hi.
+__host__ __device__ __forceinline__ dd dd_div(dd a, dd b) {
+    const float r0 = dd_rcp_seed(b.hi);
+    const float q1 = a.hi * r0;
+    const dd p = two_prod(q1, b.hi);
+    const float rem = ((a.hi - p.hi) - p.lo) + fmaf(-q1, b.lo, a.lo);
+    return fast_two_sum(q1, rem * r0);
+}
+
 // 1 / a for a != 0: one Newton step r0 (1 + e), e = 1 - a r0.
 __host__ __device__ __forceinline__ dd dd_rcp(dd a) {
     const float r0 = dd_rcp_seed(a.hi);

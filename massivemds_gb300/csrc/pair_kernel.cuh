@@ -689,7 +689,7 @@ struct PairMathF64 {
 // row sums of row i and the column sums of column j.
 template <int P, bool TRUNC, bool MASKED>
 __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P], dd dA, dd dB, bool vA, bool vB,
-                                            dd sqrt_tau, dd inv_sqrt_tau, const float* tab, dd (&racc)[P],
+                                            dd sqrt_tau, const float* tab, dd (&racc)[P],
                                             dd (&cacc)[P], dd& r2, dd& prod, dd& prodm) {
     dd dx[P];
 #pragma unroll
@@ -717,7 +717,7 @@ __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P]
         } else {
             prod = dd_mul(prod, cdf);
         }
-        t = dd_mul(dd_mul(pdf, rs), dd_mul(dd_rcp(cdf), inv_sqrt_tau));
+        t = dd_div(dd_mul(pdf, rs), dd_mul(cdf, sqrt_tau));
     }
     if (!MASKED || vA) {
         const dd nc = dd_sub(t, dd_mul(resA, rs));
@@ -762,10 +762,9 @@ struct PairMathDD {
         double l2, l1;  // as PairMathF64
         int since_fold;
     };
-    dd sqrt_tau, inv_sqrt_tau;
+    dd sqrt_tau;
 
-    __device__ explicit PairMathDD(const PairArgs& a)
-        : sqrt_tau(dd_from_double(a.sqrt_tau)), inv_sqrt_tau(dd_from_double(1.0 / a.sqrt_tau)) {}
+    __device__ explicit PairMathDD(const PairArgs& a) : sqrt_tau(dd_from_double(a.sqrt_tau)) {}
 
     __device__ static float* table() {
         __shared__ __align__(16) float tab[TRUNC ? kNormalDDFloats : 4];
@@ -832,7 +831,7 @@ struct PairMathDD {
                     vA = ok && (a.hi == a.hi);
                     vB = ok && (bb.hi == bb.hi);
                 }
-                pair_dd_sym<P, TRUNC, MASKED>(xi, cols.xj[c], a, bb, vA, vB, sqrt_tau, inv_sqrt_tau, tab, racc,
+                pair_dd_sym<P, TRUNC, MASKED>(xi, cols.xj[c], a, bb, vA, vB, sqrt_tau, tab, racc,
                                               cols.acc[c], s.r2, s.prod, prodm);
             }
 #pragma unroll

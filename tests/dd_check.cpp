@@ -22,7 +22,7 @@ static long double ld(dd a) { return (long double)a.hi + (long double)a.lo; }
 int main() {
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> uni(-4.0, 4.0);
-    long double e_add = 0, e_mul = 0, e_sqr = 0, e_fma = 0, e_rsq = 0, e_rcp = 0, e_split = 0;
+    long double e_add = 0, e_mul = 0, e_sqr = 0, e_fma = 0, e_rsq = 0, e_rcp = 0, e_div = 0, e_split = 0;
     for (int t = 0; t < 200000; ++t) {
         const double x = uni(rng), y = uni(rng), w = uni(rng);
         const dd a = dd_from_double(x), b = dd_from_double(y), c = dd_from_double(w);
@@ -37,6 +37,7 @@ int main() {
         const dd pa = dd_from_double((double)ax);
         e_rsq = std::max(e_rsq, std::fabs(ld(dd_rsqrt(pa)) * std::sqrt(ld(pa)) - 1.0L));
         e_rcp = std::max(e_rcp, std::fabs(ld(dd_rcp(a)) * A - 1.0L));
+        if (std::fabs(A) > 1e-3L) e_div = std::max(e_div, std::fabs(ld(dd_div(b, a)) * A / B - 1.0L));
     }
     // accumulators: 20 000 products of mixed sign (a row's gradient sum) and
     // squares (the likelihood's sum), against long double, relative to sum |terms|
@@ -68,6 +69,7 @@ int main() {
     report("fma", e_fma, 2e-14L);
     report("rsqrt", e_rsq, 1e-13L);
     report("rcp", e_rcp, 1e-13L);
+    report("div", e_div, 1e-13L);
 
     static float tab[kNormalDDFloats];
     normal_dd_table(tab);
