@@ -120,6 +120,22 @@ def test_sizes_and_edges(mode, n):
         assert grad_rel(g, g_ref) < TOL_GRAD, trunc
 
 
+def test_single_location_and_fp32_input():
+    """N = 1 (no pair: zero sum and gradient), and FP32 input data widened into
+    the FP64-stored double-float layout."""
+    e = make("dd", 1, 2, True, np.zeros((1, 1)), np.ones((1, 2)), 1.0)
+    assert e.getSumOfIncrements() == 0.0 and np.all(e.getLogLikelihoodGradient() == 0.0)
+    e.close()
+    n, p, tau = 300, 2, 1.1
+    delta, x = inputs(n, p, seed=63, nans=3)
+    d32 = delta.astype(np.float32)
+    s, g, s_ref, g_ref = check("dd", n, p, True, d32, x, tau)
+    s_ref = oracle.sum_of_increments(d32.astype(np.float64), x, tau)
+    g_ref = oracle.gradient(d32.astype(np.float64), x, tau)
+    assert rel(s, s_ref) < TOL_SUM
+    assert grad_rel(g, g_ref) < TOL_GRAD
+
+
 @pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("p", [1, 3, 4, 5, 6])
 def test_dimensions(mode, p):
