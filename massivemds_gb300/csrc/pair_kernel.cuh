@@ -88,6 +88,9 @@ constexpr int kPairMaxP64 = 6;   // FP64 pair math (one CTA per SM, pair_min_cta
 #ifndef MDSX_FINISH_COL_CHUNK
 #define MDSX_FINISH_COL_CHUNK 8  // column-partial loads in flight per finish thread
 #endif
+#ifndef MDSX_PAIR_ROTATE_ISSUER
+#define MDSX_PAIR_ROTATE_ISSUER 1  // single-instance pair kernel: unit m's copies issued by warp m % 8
+#endif
 #ifndef MDSX_PAIR_EARLY_RELEASE
 #define MDSX_PAIR_EARLY_RELEASE 1  // FP32 packs of rows: operands to registers, stage released before the math
 #endif
@@ -1021,8 +1024,12 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
     M::prologue(a);
     __syncthreads();
 
-    // Copy issue state (thread 0 only): next unit to issue and its (J, I).
-    const bool issuer = threadIdx.x == 0;
+    // Copy issue state, kept by lane 0 of every warp: next unit and its (J, I).
+    // Unit m is issued by warp m % 8 (MDSX_PAIR_ROTATE_ISSUER; else warp 0
+    // issues all), so the copy-issue work does not lengthen one warp's path.
+    // Deadlock-free: the slowest warp's next unit k was issued by a warp that
+    // has passed step k - S + 1, and its stage was released by every warp.
+    const bool issuer = MDSX_PAIR_ROTATE_ISSUER ? lane == 0 : threadIdx.x == 0;
     int issued = 0;
     int pJ = J_first;
     int pI = 4 * J_first + (int)(u_begin - pair_units_before(J_first, a.nc));
@@ -1036,8 +1043,9 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
     auto top_up = [&](int k) {
         while (issue_ok && issued < K && issued <= k + S - 1) {
             const int m = issued;
+            const bool mine = !MDSX_PAIR_ROTATE_ISSUER || m % kPairWarps == warp;
             const int stage = m % S;
-            if (m >= S) {
+            if (mine && m >= S) {
                 const uint32_t par = ((uint32_t)(m / S) & 1u) ^ 1u;
                 if (m <= k + S - 2) {
                     if (!mbar_wait_bounded(&empty[stage], par, a.err, kDevTimeoutEmpty)) {
@@ -1048,19 +1056,23 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
                     break;
                 }
             }
-            unsigned char* st = smem + stage * Shape::kStageBytes;
             const bool new_j = M::kXJEveryUnit || pJ != pJ_loaded;
-            const uint32_t bytes =
-                Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
-            mbar_arrive_expect_tx(&full[stage], bytes);
-            // delta is read once: evict it first, keeping the partials in L2 for the finish kernel
+            if (mine) {
+                unsigned char* st = smem + stage * Shape::kStageBytes;
+                const uint32_t bytes =
+                    Shape::kBBytes + Shape::kABytes + Shape::kXIBytes + (new_j ? Shape::kXJBytes : 0);
+                mbar_arrive_expect_tx(&full[stage], bytes);
+                // delta is read once: evict it first, keeping the partials in L2 for the finish kernel
 #pragma unroll
-            for (int bx = 0; bx < Shape::kBBoxes; ++bx)
-                tma_load_2d_hint(st + bx * (Shape::kBBytes / Shape::kBBoxes), &tmap_b,
-                                 pI * kPairRows + bx * Shape::kBBoxCols, pJ * kPairCols, &full[stage], evict_first);
-            tma_load_2d_hint(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage], evict_first);
-            tma_load_2d(st + Shape::kXIOffset, &tmap_xi, pI * kPairRows, 0, &full[stage]);
-            if (new_j) tma_load_2d(st + Shape::kXJOffset, &tmap_xj, pJ * kPairCols, 0, &full[stage]);
+                for (int bx = 0; bx < Shape::kBBoxes; ++bx)
+                    tma_load_2d_hint(st + bx * (Shape::kBBytes / Shape::kBBoxes), &tmap_b,
+                                     pI * kPairRows + bx * Shape::kBBoxCols, pJ * kPairCols, &full[stage],
+                                     evict_first);
+                tma_load_2d_hint(st + Shape::kBBytes, &tmap_a, pJ * kPairCols, pI * kPairRows, &full[stage],
+                                 evict_first);
+                tma_load_2d(st + Shape::kXIOffset, &tmap_xi, pI * kPairRows, 0, &full[stage]);
+                if (new_j) tma_load_2d(st + Shape::kXJOffset, &tmap_xj, pJ * kPairCols, 0, &full[stage]);
+            }
             pJ_loaded = pJ;
             if (++pI == a.nc) {
                 ++pJ;
@@ -1103,8 +1115,10 @@ __global__ void __launch_bounds__(kPairThreads, pair_min_ctas_of<P, M>())
     // The finish kernel may be scheduled now; it waits for this grid to complete.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (issuer) {
-        // Copies still in flight (only after a failed wait): let them land before the CTA exits.
-        for (int m = k; m < issued; ++m) mbar_wait_time_only(&full[m % S], (uint32_t)(m / S) & 1u);
+        // Copies still in flight (only after a failed wait): let this warp's land before the CTA exits.
+        for (int m = k; m < issued; ++m)
+            if (!MDSX_PAIR_ROTATE_ISSUER || m % kPairWarps == warp)
+                mbar_wait_time_only(&full[m % S], (uint32_t)(m / S) & 1u);
     }
     if (!alive) return;
 
