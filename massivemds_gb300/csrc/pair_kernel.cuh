@@ -24,9 +24,10 @@
 //   x_I = P location rows + the flag row, 32 columns (compute type)
 //   x_J = the same over J's 128 columns, with the first unit of each J
 // into a ring of PairShape::kStages stages (mbarrier full/empty pairs). Lane 0
-// of warp 0 issues the copies between its own units, so all 8 warps of a CTA
-// compute and 2 CTAs of 256 threads fit an SM at 128 registers (P = 4, 6: one
-// CTA per SM, pair_min_ctas).
+// of warp m % 8 issues unit m's copies between its own units (the batch
+// kernel: lane 0 of warp 0 for every unit), so all 8 warps of a CTA compute and
+// 2 CTAs of 256 threads fit an SM at 128 registers (P = 4, 6: one CTA per SM,
+// pair_min_ctas).
 //
 // Consumer warp w owns rows 4w .. 4w+3 of the chunk and lane l the columns
 // l, l+32, l+64, l+96 of the block. B gives a lane its four rows of column j
