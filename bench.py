@@ -58,7 +58,8 @@ PARITY_TOL = {"f32": 1e-5, "f64_sum": 1e-10, "f64_grad": 1e-9}
 
 
 def workload(n: int, precision: str = "f32", evals: int = EVALS_PER_STEP) -> str:
-    math = "FP32 pairs + FP64 reductions" if precision == "f32" else "FP64 pairs (DELTA_F32 mode)"
+    math = {"f32": "FP32 pairs + FP64 reductions", "f64": "FP64 pairs (DELTA_F32 mode)",
+            "dd": "double-float pairs on the FP32 pipes (DOUBLE_FLOAT | DELTA_F32), FP64 bars"}[precision]
     return (f"fused loglik+grad sweep, N={n}, P=2, tau=2, truncation, delta FP32-stored ({n * n * 4 / 1e9:.2f} GB), "
             f"{math}, {evals} eval{'s' if evals != 1 else ''} per step at fresh locations")
 
@@ -74,9 +75,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mdsx", choices=["mdsx", "reference"])
     ap.add_argument("--n", type=int, default=N)
-    ap.add_argument("--precision", default="f32", choices=["f32", "f64"],
-                    help="pair arithmetic: f32 (the headline; FP32 pairs, FP64 reductions) or f64 (FP64 pairs over "
-                         "the same FP32-stored delta; bound by the FP64 pipe, 10 evaluations per step)")
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64", "dd"],
+                    help="pair arithmetic: f32 (the headline; FP32 pairs, FP64 reductions), f64 (FP64 pairs over "
+                         "the same FP32-stored delta; bound by the FP64 pipe, 10 evaluations per step) or dd "
+                         "(double-float pairs on the FP32 pipes at the FP64 bars, 50 evaluations per step)")
     ap.add_argument("--schedule", default="pairs", choices=["pairs", "rows"],
                     help="sweep schedule: each unordered pair once (default) or the row-block schedule")
     ap.add_argument("--workload", default="sweep", choices=["sweep", "c1", "c3"],
@@ -788,10 +790,12 @@ def run_mdsx(args):
 
     sections = {s for s in args.sections.split(",") if s}
     n = args.n
-    f64 = args.precision == "f64"
-    evals = 10 if f64 else EVALS_PER_STEP
+    f64 = args.precision in ("f64", "dd")  # FP64-accurate results, held to the FP64 bars
+    evals = {"f64": 10, "dd": 50}.get(args.precision, EVALS_PER_STEP)
     delta = make_delta(n)
-    eng = m.Engine(P, n, (m.flags.DELTA_F32 if f64 else m.flags.FLOAT) | m.flags.LEFT_TRUNCATION, local)
+    flags = {"f32": m.flags.FLOAT, "f64": m.flags.DELTA_F32,
+             "dd": m.flags.DELTA_F32 | m.flags.DOUBLE_FLOAT}[args.precision]
+    eng = m.Engine(P, n, flags | m.flags.LEFT_TRUNCATION, local)
     eng.set_sweep_schedule(m.flags.SWEEP_PAIRS if args.schedule == "pairs" else m.flags.SWEEP_ROWS)
     eng.setPairwiseData(delta)
     eng.setParameters([TAU])
@@ -880,7 +884,10 @@ def run_mdsx(args):
     bytes_per_launch = float(n) * n * 4 + 2.0 * n * P * 4
     achieved = bytes_per_launch / (kernel_ms / 1000.0) / 1e9
     traffic = profiled_traffic(args.schedule) if n == N else None  # the committed captures are of N = 20000
-    if f64:
+    if args.precision == "dd":
+        kernel_name = "pair_kernel<2,true,PairMathDD<float>> + pair_finish_kernel<2,double>"
+        traffic = None  # FP32-pipe bound: the HBM fraction below is small by construction
+    elif f64:
         kernel_name = ("pair_kernel<2,true,PairMathF64<float>> + pair_finish_kernel<2,double>"
                        if args.schedule == "pairs" else "sweep_kernel<double,float,2,true>")
         traffic = None  # FP64-pipe bound: the HBM fraction below is small by construction
