@@ -116,6 +116,13 @@ __host__ __device__ __forceinline__ void dd_acc_sqr(dd& acc, dd a) {
     acc.lo += s.lo + fmaf(a.hi + a.hi, a.lo, p.lo);
 }
 
+// acc += a, with the same unnormalised accumulator as dd_acc_fma.
+__host__ __device__ __forceinline__ void dd_acc_add(dd& acc, dd a) {
+    const dd s = two_sum(acc.hi, a.hi);
+    acc.hi = s.hi;
+    acc.lo += s.lo + a.lo;
+}
+
 __host__ __device__ __forceinline__ dd dd_renorm(dd a) { return fast_two_sum(a.hi, a.lo); }
 
 // c + a * b, rounded once to double-float.

@@ -693,8 +693,8 @@ struct PairMathF64 {
 // row sums of row i and the column sums of column j.
 template <int P, bool TRUNC, bool MASKED>
 __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P], dd dA, dd dB, bool vA, bool vB,
-                                            dd sqrt_tau, const float* tab, dd (&racc)[P],
-                                            dd (&cacc)[P], dd& r2, dd& prod, dd& prodm) {
+                                            dd sqrt_tau, dd inv_sqrt_tau, const float* tab, dd (&racc)[P],
+                                            dd (&cacc)[P], dd& r2, dd& lf, dd& lm) {
     dd dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = dd_sub(xi[q], xj[q]);  // normalised: products drop lo * lo
@@ -711,17 +711,17 @@ __device__ __forceinline__ void pair_dd_sym(const dd (&xi)[P], const dd (&xj)[P]
     if (!MASKED || vB) dd_acc_sqr(r2, resB);
     dd t = dd_of(0.0f);
     if (TRUNC) {
-        const dd z = dd_mul(d, sqrt_tau);
-        dd q, pdf;
-        normal_dd(z, tab, q, pdf);
-        const dd cdf = dd_add_f(dd_neg(q), 1.0f);
+        // log Phi(z) straight into the likelihood sums (the fast path counts it
+        // once for both directions) and phi / Phi for the gradient term
+        dd lc, ratio;
+        normal_dd(dd_mul(d, sqrt_tau), tab, lc, ratio);
         if (MASKED) {
-            if (vA) prodm = dd_mul(prodm, cdf);
-            if (vB) prodm = dd_mul(prodm, cdf);
+            if (vA) dd_acc_add(lm, lc);
+            if (vB) dd_acc_add(lm, lc);
         } else {
-            prod = dd_mul(prod, cdf);
+            dd_acc_add(lf, lc);
         }
-        t = dd_div(dd_mul(pdf, rs), dd_mul(cdf, sqrt_tau));
+        t = dd_mul(dd_mul(ratio, rs), inv_sqrt_tau);
     }
     if (!MASKED || vA) {
         const dd nc = dd_sub(t, dd_mul(resA, rs));
@@ -755,20 +755,19 @@ struct PairMathDD {
     // 4.28 -> 3.95 ms (200 bytes spilled) at N = 20 000. FP64-stored delta fits
     // one CTA per SM, which keeps up to 255 registers (P = 3 at 128: +21 %).
     static constexpr int kMinCtas = sizeof(DeltaT) == 4 && P <= MDSX_DD_TWO_CTAS_MAX_P ? 2 : 1;
-    // 16 factors >= 1/2 per unit on the fast path: >= 2^-64 per fold, well inside FP32's range
-    static constexpr int kFoldUnits = 4;
     struct Cols {
         dd xj[4][P];
         dd acc[4][P];
     };
     struct Sums {
-        dd r2, prod;
-        double l2, l1;  // as PairMathF64
-        int since_fold;
+        dd r2;
+        dd lf;  // log Phi over the fast path's unordered pairs (counted for both directions)
+        dd lm;  // log Phi over the masked path's valid ordered pairs
     };
-    dd sqrt_tau;
+    dd sqrt_tau, inv_sqrt_tau;
 
-    __device__ explicit PairMathDD(const PairArgs& a) : sqrt_tau(dd_from_double(a.sqrt_tau)) {}
+    __device__ explicit PairMathDD(const PairArgs& a)
+        : sqrt_tau(dd_from_double(a.sqrt_tau)), inv_sqrt_tau(dd_from_double(1.0 / a.sqrt_tau)) {}
 
     __device__ static float* table() {
         __shared__ __align__(16) float tab[TRUNC ? kNormalDDFloats : 4];
@@ -789,12 +788,7 @@ struct PairMathDD {
     __device__ static dd delta(float v) { return dd_of(v); }
     __device__ static dd delta(double v) { return slot(v); }
 
-    __device__ static void init(Sums& s) {
-        s.r2 = dd_of(0.0f);
-        s.prod = dd_of(1.0f);
-        s.l2 = s.l1 = 0.0;
-        s.since_fold = 0;
-    }
+    __device__ static void init(Sums& s) { s.r2 = s.lf = s.lm = dd_of(0.0f); }
     __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
 #pragma unroll
         for (int c = 0; c < 4; ++c)
@@ -808,7 +802,6 @@ struct PairMathDD {
     __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
                          int lane, int warp, Part (&v)[4 * P]) const {
         const float* tab = table();
-        dd prodm = dd_of(1.0f);
 #pragma unroll
         for (int k = 0; k < 4 * P; ++k) v[k] = 0.0;
         // Rows one at a time in a loop that is not unrolled (the four column
@@ -835,8 +828,8 @@ struct PairMathDD {
                     vA = ok && (a.hi == a.hi);
                     vB = ok && (bb.hi == bb.hi);
                 }
-                pair_dd_sym<P, TRUNC, MASKED>(xi, cols.xj[c], a, bb, vA, vB, sqrt_tau, tab, racc,
-                                              cols.acc[c], s.r2, s.prod, prodm);
+                pair_dd_sym<P, TRUNC, MASKED>(xi, cols.xj[c], a, bb, vA, vB, sqrt_tau, inv_sqrt_tau, tab, racc,
+                                              cols.acc[c], s.r2, s.lf, s.lm);
             }
 #pragma unroll
             for (int k = 0; k < 3 * P; ++k) v[k] = v[k + P];
@@ -845,25 +838,20 @@ struct PairMathDD {
         }
         // the long-lived accumulators: renormalised once per unit (dd_acc_fma)
         s.r2 = dd_renorm(s.r2);
+        if (TRUNC) {
+            s.lf = dd_renorm(s.lf);
+            s.lm = dd_renorm(s.lm);
+        }
 #pragma unroll
         for (int c = 0; c < 4; ++c)
 #pragma unroll
             for (int q = 0; q < P; ++q) cols.acc[c][q] = dd_renorm(cols.acc[c][q]);
-        if (MASKED && TRUNC) s.l1 += log(dd_to_double(prodm));  // <= 32 factors >= 1/2
     }
-    __device__ static void after_unit(Sums& s) {
-        if (++s.since_fold == kFoldUnits) {
-            s.since_fold = 0;
-            if (TRUNC) {
-                s.l2 += log(dd_to_double(s.prod));
-                s.prod = dd_of(1.0f);
-            }
-        }
-    }
+    __device__ static void after_unit(Sums&) {}
     __device__ static Part col_value(const Cols& cols, int c, int q) { return dd_to_double(cols.acc[c][q]); }
     __device__ static void result(Sums& s, double& r2, double& lsum) {
         r2 = dd_to_double(s.r2);
-        lsum = TRUNC ? 2.0 * (s.l2 + log(dd_to_double(s.prod))) + s.l1 : 0.0;
+        lsum = TRUNC ? 2.0 * dd_to_double(s.lf) + dd_to_double(s.lm) : 0.0;
     }
 };
 

@@ -1,5 +1,6 @@
 // Host check of the double-float arithmetic (massivemds_gb300/csrc/dd.h) and the
-// double-float normal tail table (normal_dd.h) against long double references.
+// double-float normal-tail table (normal_dd.h: log Phi and phi / Phi) against
+// long double references.
 // Prints one line per check: name, max error, bound; exits 1 if a bound fails.
 #include <cstdio>
 #include <cstdlib>
@@ -74,22 +75,23 @@ int main() {
     static float tab[kNormalDDFloats];
     normal_dd_table(tab);
     const long double inv_sqrt_2pi = 0.398942280401432677939946059934381868L;
-    long double e_q = 0, e_phi = 0, e_q_rel = 0;
+    long double e_l = 0, e_h = 0, e_h_rel = 0;
     std::uniform_real_distribution<double> zd(0.0, 9.0);
     for (int t = 0; t < 400000; ++t) {
         const double zz = t < 1000 ? t * (9.0 / 1000) : zd(rng);
         const dd z = dd_from_double(zz);
         const long double Z = ld(z);
-        dd q, phi;
-        normal_dd(z, tab, q, phi);
+        dd lc, ratio;
+        normal_dd(z, tab, lc, ratio);
         const long double Q = 0.5L * std::erfc(Z / std::sqrt(2.0L));
         const long double PHI = inv_sqrt_2pi * std::exp(-0.5L * Z * Z);
-        e_q = std::max(e_q, std::fabs(ld(q) - Q));
-        e_phi = std::max(e_phi, std::fabs(ld(phi) - PHI));
-        if (Z < 8.0L) e_q_rel = std::max(e_q_rel, std::fabs(ld(q) - Q) / Q);
+        const long double L = std::log1p(-Q), H = PHI / (1.0L - Q);
+        e_l = std::max(e_l, std::fabs(ld(lc) - L));
+        e_h = std::max(e_h, std::fabs(ld(ratio) - H));
+        if (Z < 8.0L) e_h_rel = std::max(e_h_rel, std::fabs(ld(ratio) - H) / H);
     }
-    report("normal_Q_abs", e_q, 5e-14L);
-    report("normal_Q_rel_z<8", e_q_rel, 5e-10L);
-    report("normal_phi_abs", e_phi, 5e-14L);
+    report("normal_logcdf_abs", e_l, 5e-14L);
+    report("normal_ratio_abs", e_h, 5e-14L);
+    report("normal_ratio_rel_z<8", e_h_rel, 5e-10L);
     return failures ? 1 : 0;
 }
