@@ -118,6 +118,7 @@ void free_all(mdsx_engine* e) {
     cudaFree(e->d_pair_jfirst);
     cudaFree(e->d_pair_jslots);
     cudaFree(e->d_normal_table);
+    cudaFree(e->d_normal_table_f64);
     if (e->h_out) cudaFreeHost(e->h_out);
     if (e->h_xstage) cudaFreeHost(e->h_xstage);
     if (e->h_grad) cudaFreeHost(e->h_grad);
@@ -243,6 +244,14 @@ int plan_and_allocate(mdsx_engine* e) {
         // 1.8x truncated (N = 20 000, P = 2).
         if (e->trunc || e->mode != Mode::kF32) e->schedule = MDSX_SWEEP_PAIRS;
     }
+    // the FP64 pair math's normal-tail table (also kept for a later switch to the pair schedule)
+    if (!e->dd && e->mode != Mode::kF32 && e->trunc && e->d_rowpart) {
+        std::vector<double> table(mdsx::kNormalF64Doubles);
+        mdsx::normal_f64_table(table.data());
+        MDSX_CUDA(e, mdsx::device_malloc(&e->d_normal_table_f64, table.size() * sizeof(double)));
+        MDSX_CUDA(e, cudaMemcpy(e->d_normal_table_f64, table.data(), table.size() * sizeof(double),
+                                cudaMemcpyHostToDevice));
+    }
     if (e->dd) {
         if (e->schedule != MDSX_SWEEP_PAIRS)
             return fail(e, MDSX_EUNSUPPORTED,
@@ -356,6 +365,7 @@ mdsx::PairArgs make_pair_args(mdsx_engine* e) {
     pa.sums_out = a.sums_out;
     pa.err = a.err;
     pa.normal_table = e->d_normal_table;
+    pa.normal_table_f64 = e->d_normal_table_f64;
     return pa;
 }
 

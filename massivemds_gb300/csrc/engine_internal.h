@@ -29,7 +29,8 @@ struct mdsx_engine {
     // `mode`, with FP64 delta and the locations held as (hi, lo) float pairs in
     // their 8-byte slots; unordered-pair schedule only.
     bool dd = false;
-    float* d_normal_table = nullptr;  // normal_dd_table, with truncation
+    float* d_normal_table = nullptr;       // normal_dd_table (double-float pair math, truncation)
+    double* d_normal_table_f64 = nullptr;  // normal_f64_table (FP64 pair math, truncation)
 
     cudaStream_t own_stream = nullptr;
     cudaEvent_t h2d_done = nullptr;  // recorded after the copy of a caller's host locations

@@ -17,7 +17,8 @@
 // (z > 8.5 + 1/64) |log Phi| < 1e-17 and H < 1e-16 are returned as 0.
 //
 // The table is computed on the host from the C library's erfc, exp and log1p in
-// long double (normal_dd_table) and copied to shared memory by each CTA.
+// long double (normal_dd_table) and copied to shared memory by each CTA. The
+// FP64 pair math uses the same series in double (normal_f64_table, normal_f64).
 #pragma once
 
 #include <cmath>
@@ -31,24 +32,33 @@ constexpr int kNormalDDEntries = 273;    // z_k = 0 .. 8.5
 constexpr int kNormalDDStride = 20;      // floats per entry (five 16-byte groups)
 constexpr int kNormalDDFloats = kNormalDDEntries * kNormalDDStride;
 
+constexpr int kNormalTerms = 7;           // coefficients per series
+constexpr int kNormalF64Stride = 16;      // doubles per entry of the FP64 table: l0..l6, 0, h0..h6, 0
+constexpr int kNormalF64Doubles = kNormalDDEntries * kNormalF64Stride;
+
+// The series coefficients l_m, h_m about z_k = k / 32 (long double).
+inline void normal_series(int k, long double (&l)[kNormalTerms], long double (&h)[kNormalTerms]) {
+    const long double inv_sqrt_2pi = 0.398942280401432677939946059934381868L;
+    const long double z = (long double)k / kNormalDDPerUnit;
+    const long double phi = inv_sqrt_2pi * std::exp(-0.5L * z * z);
+    const long double q = 0.5L * std::erfc(z / std::sqrt(2.0L));
+    h[0] = phi / (1.0L - q);
+    for (int m = 0; m + 1 < kNormalTerms; ++m) {
+        long double conv = 0.0L;
+        for (int i = 0; i <= m; ++i) conv += h[i] * h[m - i];
+        h[m + 1] = (-z * h[m] - (m > 0 ? h[m - 1] : 0.0L) - conv) / (long double)(m + 1);
+    }
+    l[0] = std::log1p(-q);
+    for (int m = 1; m < kNormalTerms; ++m) l[m] = h[m - 1] / (long double)m;
+}
+
 // Entry layout (floats): l0 (hi, lo), l1 (hi, lo), l2 (hi, lo), l3, l4, l5, l6,
 // h0 (hi, lo), h1 (hi, lo), h2 (hi, lo), h3, h4, h5, h6.
 inline void normal_dd_table(float* out) {
-    const long double inv_sqrt_2pi = 0.398942280401432677939946059934381868L;
-    constexpr int M = 7;  // coefficients per series
+    constexpr int M = kNormalTerms;
     for (int k = 0; k < kNormalDDEntries; ++k) {
-        const long double z = (long double)k / kNormalDDPerUnit;
-        const long double phi = inv_sqrt_2pi * std::exp(-0.5L * z * z);
-        const long double q = 0.5L * std::erfc(z / std::sqrt(2.0L));
-        long double h[M], l[M];
-        h[0] = phi / (1.0L - q);
-        for (int m = 0; m + 1 < M; ++m) {
-            long double conv = 0.0L;
-            for (int i = 0; i <= m; ++i) conv += h[i] * h[m - i];
-            h[m + 1] = (-z * h[m] - (m > 0 ? h[m - 1] : 0.0L) - conv) / (long double)(m + 1);
-        }
-        l[0] = std::log1p(-q);
-        for (int m = 1; m < M; ++m) l[m] = h[m - 1] / (long double)m;
+        long double l[M], h[M];
+        normal_series(k, l, h);
         float* t = out + k * kNormalDDStride;
         for (int m = 0; m < 3; ++m) {
             const dd lm = dd_from_double((double)l[m]);
@@ -84,6 +94,34 @@ __host__ __device__ __forceinline__ void normal_dd(dd z, const float* tab, dd& l
     p = dd_add(dd_of(t[14], t[15]), dd_mul_f(u, r));
     p = dd_fma(u, p, dd_of(t[12], t[13]));
     ratio = dd_fma(u, p, dd_of(t[10], t[11]));
+}
+
+inline void normal_f64_table(double* out) {
+    for (int k = 0; k < kNormalDDEntries; ++k) {
+        long double l[kNormalTerms], h[kNormalTerms];
+        normal_series(k, l, h);
+        double* t = out + k * kNormalF64Stride;
+        for (int m = 0; m < kNormalF64Stride; ++m) t[m] = 0.0;
+        for (int m = 0; m < kNormalTerms; ++m) {
+            t[m] = (double)l[m];
+            t[8 + m] = (double)h[m];
+        }
+    }
+}
+
+// log Phi(z) and phi(z) / Phi(z) in FP64 for z >= 0 from the table `tab`
+// (Horner in double; within 2e-16 of the exact values, tests/dd_check.cpp).
+__host__ __device__ __forceinline__ void normal_f64(double z, const double* tab, double& log_cdf, double& ratio) {
+    const int k = (int)fma(z, (double)kNormalDDPerUnit, 0.5);
+    if (k >= kNormalDDEntries) {
+        log_cdf = 0.0;
+        ratio = 0.0;
+        return;
+    }
+    const double* t = tab + k * kNormalF64Stride;
+    const double u = z - (double)k * (1.0 / kNormalDDPerUnit);  // exact (Sterbenz)
+    log_cdf = fma(fma(fma(fma(fma(fma(t[6], u, t[5]), u, t[4]), u, t[3]), u, t[2]), u, t[1]), u, t[0]);
+    ratio = fma(fma(fma(fma(fma(fma(t[14], u, t[13]), u, t[12]), u, t[11]), u, t[10]), u, t[9]), u, t[8]);
 }
 
 }  // namespace mdsx

@@ -152,7 +152,8 @@ struct PairArgs {
     int* err;
     int leapfrog;       // nonzero: the finish applies `leap` to its rows
     PairLeapfrog leap;
-    const float* normal_table;  // double-float pair math with truncation: normal_dd_table (kNormalDDFloats)
+    const float* normal_table;       // double-float pair math with truncation: normal_dd_table (kNormalDDFloats)
+    const double* normal_table_f64;  // FP64 pair math with truncation: normal_f64_table (kNormalF64Doubles)
 };
 
 // Units of the column blocks before J: sum over J' < J of (nc - 4 J').
@@ -535,17 +536,17 @@ using PairMathF32For =
 
 // ------------------------------------------------------------ FP64 pair math
 
-// One unordered pair {i, j} in FP64 (rsqrt_f64, rcp_f64, normal_cdf_pdf_f64 with
-// CUDA's exp), both directions: dA = delta_ij, dB = delta_ji.
+// One unordered pair {i, j} in FP64 (rsqrt_f64; log Phi and phi / Phi from
+// the Taylor table of normal_f64), both directions: dA = delta_ij, dB = delta_ji.
 // With c = [(delta - d) - phi(z) / (Phi(z) sqrt(tau))] / d the (i, j) term
 // -c_A (x_i - x_j) accumulates into racc and the (j, i) term -c_B (x_i - x_j)
-// into cacc (signs as in the FP32 policy). Fast path: Phi multiplies into prod
-// once and counts for both directions; masked path: each valid direction into
-// prodm. Phi >= 1/2 for d >= 0.
+// into cacc (signs as in the FP32 policy). Fast path: log Phi adds into lf once
+// and counts for both directions; masked path: each valid direction into lm.
 template <int P, bool TRUNC, bool MASKED>
 __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double (&xj)[P], double dA, double dB,
-                                             bool vA, bool vB, double sqrt_tau, double (&racc)[P],
-                                             double (&cacc)[P], double& r2, double& prod, double& prodm) {
+                                             bool vA, bool vB, double sqrt_tau, double inv_sqrt_tau,
+                                             const double* tab, double (&racc)[P], double (&cacc)[P], double& r2,
+                                             double& lf, double& lm) {
     double dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = xi[q] - xj[q];
@@ -562,16 +563,15 @@ __device__ __forceinline__ void pair_f64_sym(const double (&xi)[P], const double
     if (!MASKED || vB) r2 = fma(resB, resB, r2);
     double t = 0.0;
     if (TRUNC) {
-        const double z = d * sqrt_tau;
-        double cdf, pdf;
-        normal_cdf_pdf_f64(z, cdf, pdf);
+        double lc, ratio;
+        normal_f64(d * sqrt_tau, tab, lc, ratio);
         if (MASKED) {
-            if (vA) prodm *= cdf;
-            if (vB) prodm *= cdf;
+            if (vA) lm += lc;
+            if (vB) lm += lc;
         } else {
-            prod *= cdf;
+            lf += lc;
         }
-        t = pdf * rs * rcp_f64(cdf * sqrt_tau);
+        t = ratio * rs * inv_sqrt_tau;
     }
     if (!MASKED || vA) {
         const double nc = fma(-resA, rs, t);
@@ -600,36 +600,42 @@ __device__ __forceinline__ S pair_b_value(const S* sB, int lane, int warp, int c
 }
 
 // FP64 policy: scalar FP64 pairs over FP32- or FP64-stored delta and FP64 locations;
-// FP64 partials; Phi multiplied into per-lane products, log taken every
-// kFoldUnits units.
+// FP64 partials; log Phi summed per lane. With truncation each CTA copies the
+// FP64 normal-tail table (normal_f64_table) into shared memory first.
 template <int P, bool TRUNC, typename DeltaT>
 struct PairMathF64 {
     using X = double;
     using S = DeltaT;  // float (DELTA_F32 mode) or double (FP64 mode)
     using Part = double;
     static constexpr bool kXJEveryUnit = false;
-    __device__ static void prologue(const PairArgs&) {}  // no shared tables
     static constexpr int kMinCtas = 0;  // pair_min_ctas_of decides
     static constexpr bool kEarlyRelease = false;  // bound by the FP64 pipe: reads its operands from the stage
-    static constexpr int kFoldUnits = 32;  // fast path: 16 factors >= 1/2 per unit stay above 2^-512
     struct Cols {
         double xj[4][P];
         double acc[4][P];
     };
     struct Sums {
-        double r2, prod, l2, l1;  // l2: log of Phi products counted for both directions; l1: once
-        int since_fold;
+        double r2;
+        double lf;  // log Phi over the fast path's unordered pairs (counted for both directions)
+        double lm;  // log Phi over the masked path's valid ordered pairs
     };
-    double sqrt_tau;
+    double sqrt_tau, inv_sqrt_tau;
 
-    __device__ explicit PairMathF64(const PairArgs& a) : sqrt_tau(a.sqrt_tau) {}
+    __device__ explicit PairMathF64(const PairArgs& a) : sqrt_tau(a.sqrt_tau), inv_sqrt_tau(1.0 / a.sqrt_tau) {}
 
-    __device__ static void init(Sums& s) {
-        s.r2 = 0.0;
-        s.prod = 1.0;
-        s.l2 = s.l1 = 0.0;
-        s.since_fold = 0;
+    __device__ static double* table() {
+        __shared__ __align__(16) double tab[TRUNC ? kNormalF64Doubles : 2];
+        return tab;
     }
+    // Every thread of the CTA takes part; the kernel synchronises after it.
+    __device__ static void prologue(const PairArgs& a) {
+        if (!TRUNC) return;
+        const double2* src = reinterpret_cast<const double2*>(a.normal_table_f64);
+        double2* dst = reinterpret_cast<double2*>(table());
+        for (int k = threadIdx.x; k < kNormalF64Doubles / 2; k += blockDim.x) dst[k] = __ldg(&src[k]);
+    }
+
+    __device__ static void init(Sums& s) { s.r2 = s.lf = s.lm = 0.0; }
     __device__ static void begin_block(Cols& cols, const X* sXJ, int lane) {
 #pragma unroll
         for (int c = 0; c < 4; ++c)
@@ -643,7 +649,7 @@ struct PairMathF64 {
     template <bool MASKED>
     __device__ void unit(const S* sA, const S* sB, const X* sXI, Cols& cols, Sums& s, int i0, int j0, int n,
                          int lane, int warp, Part (&v)[4 * P]) const {
-        double prodm = 1.0;
+        const double* tab = table();
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             double xi[P], racc[P];
@@ -664,27 +670,18 @@ struct PairMathF64 {
                     vA = ok && (a == a);
                     vB = ok && (bb == bb);
                 }
-                pair_f64_sym<P, TRUNC, MASKED>(xi, cols.xj[c], (double)a, (double)bb, vA, vB, sqrt_tau, racc,
-                                               cols.acc[c], s.r2, s.prod, prodm);
+                pair_f64_sym<P, TRUNC, MASKED>(xi, cols.xj[c], (double)a, (double)bb, vA, vB, sqrt_tau,
+                                               inv_sqrt_tau, tab, racc, cols.acc[c], s.r2, s.lf, s.lm);
             }
 #pragma unroll
             for (int q = 0; q < P; ++q) v[r * P + q] = racc[q];
         }
-        if (MASKED && TRUNC) s.l1 += log(prodm);  // <= 32 factors >= 1/2
     }
-    __device__ static void after_unit(Sums& s) {
-        if (++s.since_fold == kFoldUnits) {
-            s.since_fold = 0;
-            if (TRUNC) {
-                s.l2 += log(s.prod);
-                s.prod = 1.0;
-            }
-        }
-    }
+    __device__ static void after_unit(Sums&) {}
     __device__ static Part col_value(const Cols& cols, int c, int q) { return cols.acc[c][q]; }
     __device__ static void result(Sums& s, double& r2, double& lsum) {
         r2 = s.r2;
-        lsum = TRUNC ? 2.0 * (s.l2 + log(s.prod)) + s.l1 : 0.0;
+        lsum = TRUNC ? 2.0 * s.lf + s.lm : 0.0;
     }
 };
 

@@ -91,6 +91,23 @@ int main() {
         if (Z < 8.0L) e_h_rel = std::max(e_h_rel, std::fabs(ld(ratio) - H) / H);
     }
     report("normal_logcdf_abs", e_l, 5e-14L);
+    {
+        static double tab64[kNormalF64Doubles];
+        normal_f64_table(tab64);
+        long double e_l64 = 0, e_h64 = 0;
+        for (int t = 0; t < 400000; ++t) {
+            const double zz = t < 1000 ? t * (9.0 / 1000) : zd(rng);
+            const long double Z = zz;
+            double lc, ratio;
+            normal_f64(zz, tab64, lc, ratio);
+            const long double Q = 0.5L * std::erfc(Z / std::sqrt(2.0L));
+            const long double PHI = inv_sqrt_2pi * std::exp(-0.5L * Z * Z);
+            e_l64 = std::max(e_l64, std::fabs((long double)lc - std::log1p(-Q)));
+            e_h64 = std::max(e_h64, std::fabs((long double)ratio - PHI / (1.0L - Q)));
+        }
+        report("normal_f64_logcdf_abs", e_l64, 5e-16L);
+        report("normal_f64_ratio_abs", e_h64, 5e-16L);
+    }
     report("normal_ratio_abs", e_h, 5e-14L);
     report("normal_ratio_rel_z<8", e_h_rel, 5e-10L);
     return failures ? 1 : 0;
