@@ -22,6 +22,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstring>
 
 #include "dd.h"
 
@@ -33,7 +34,7 @@ constexpr int kNormalDDStride = 20;      // floats per entry (five 16-byte group
 constexpr int kNormalDDFloats = kNormalDDEntries * kNormalDDStride;
 
 constexpr int kNormalTerms = 7;           // coefficients per series
-constexpr int kNormalF64Stride = 16;      // doubles per entry of the FP64 table: l0..l6, 0, h0..h6, 0
+constexpr int kNormalF64Stride = 16;      // doubles per entry of the FP64 table: l0..l6, z_k, h0..h6, 0
 constexpr int kNormalF64Doubles = kNormalDDEntries * kNormalF64Stride;
 
 // The series coefficients l_m, h_m about z_k = k / 32 (long double).
@@ -106,20 +107,33 @@ inline void normal_f64_table(double* out) {
             t[m] = (double)l[m];
             t[8 + m] = (double)h[m];
         }
+        t[7] = (double)k / kNormalDDPerUnit;
     }
+}
+
+// The grid index k = round(32 z) for 0 <= z < 8.5 + 1/64, by adding 1.5 * 2^52:
+// the sum's low word then holds k, with no FP64 conversion instruction.
+__host__ __device__ __forceinline__ int normal_f64_index(double z) {
+    const double t = fma(z, (double)kNormalDDPerUnit, 6755399441055744.0);
+#ifdef __CUDA_ARCH__
+    return __double2loint(t);
+#else
+    unsigned long long b;
+    std::memcpy(&b, &t, sizeof b);
+    return (int)(unsigned)(b & 0xffffffffull);
+#endif
 }
 
 // log Phi(z) and phi(z) / Phi(z) in FP64 for z >= 0 from the table `tab`
 // (Horner in double; within 2e-16 of the exact values, tests/dd_check.cpp).
 __host__ __device__ __forceinline__ void normal_f64(double z, const double* tab, double& log_cdf, double& ratio) {
-    const int k = (int)fma(z, (double)kNormalDDPerUnit, 0.5);
-    if (k >= kNormalDDEntries) {
+    if (!(z < 8.5 + 1.0 / (2 * kNormalDDPerUnit))) {  // beyond the grid (or NaN)
         log_cdf = 0.0;
         ratio = 0.0;
         return;
     }
-    const double* t = tab + k * kNormalF64Stride;
-    const double u = z - (double)k * (1.0 / kNormalDDPerUnit);  // exact (Sterbenz)
+    const double* t = tab + normal_f64_index(z) * kNormalF64Stride;
+    const double u = z - t[7];  // z - z_k, exact (Sterbenz)
     log_cdf = fma(fma(fma(fma(fma(fma(t[6], u, t[5]), u, t[4]), u, t[3]), u, t[2]), u, t[1]), u, t[0]);
     ratio = fma(fma(fma(fma(fma(fma(t[14], u, t[13]), u, t[12]), u, t[11]), u, t[10]), u, t[9]), u, t[8]);
 }
