@@ -244,8 +244,8 @@ int plan_and_allocate(mdsx_engine* e) {
         // 1.8x truncated (N = 20 000, P = 2).
         if (e->trunc || e->mode != Mode::kF32) e->schedule = MDSX_SWEEP_PAIRS;
     }
-    // the FP64 pair math's normal-tail table (also kept for a later switch to the pair schedule)
-    if (!e->dd && e->mode != Mode::kF32 && e->trunc && e->d_rowpart) {
+    // the FP64 math's normal-tail table (pair and row-block schedules)
+    if (!e->dd && e->mode != Mode::kF32 && e->trunc) {
         std::vector<double> table(mdsx::kNormalF64Doubles);
         mdsx::normal_f64_table(table.data());
         MDSX_CUDA(e, mdsx::device_malloc(&e->d_normal_table_f64, table.size() * sizeof(double)));
@@ -331,6 +331,7 @@ SweepArgs make_args(mdsx_engine* e) {
     a.sums_out = e->d_out;
     a.truncation = e->trunc ? 1 : 0;
     a.err = reinterpret_cast<int*>(e->d_out + 3);
+    a.normal_table_f64 = e->d_normal_table_f64;
     return a;
 }
 

@@ -41,8 +41,9 @@
 #include <cstdint>
 #include <cuda.h>
 
-#include "ptx.cuh"
+#include "normal_dd.h"
 #include "normal_mills_f64.h"
+#include "ptx.cuh"
 
 namespace mdsx {
 
@@ -57,7 +58,6 @@ constexpr int kStepCols = 128;                       // columns per stage: 32 la
 #endif
 constexpr int kStages = MDSX_STAGES;  // depth of the TMA ring
 constexpr int kLogFoldPairs = 64;
-constexpr int kLogFoldF64Stages = 64;  // FP64: 256 factors >= 1/2 per product stay above 1e-78                    // product of <= 64 factors in [1, 2] cannot overflow
 
 struct SweepArgs {
     int n;               // locations N (the columns of delta)
@@ -88,7 +88,16 @@ struct SweepArgs {
                        // [2] = getSumOfIncrements() of those sums
     int truncation;
     int* err;
+    const double* normal_table_f64;  // FP64 math with truncation: normal_f64_table (kNormalF64Doubles)
 };
+
+// The FP64 normal-tail table in shared memory (a static array of the kernel
+// that calls it; two doubles where the table is not used).
+template <bool ENABLE>
+__device__ __forceinline__ double* sweep_normal_table() {
+    __shared__ __align__(16) double tab[ENABLE ? kNormalF64Doubles : 2];
+    return tab;
+}
 
 // CTA whose unit range [c*U/G, (c+1)*U/G) holds unit u (requires G <= U).
 __host__ __device__ inline int cta_of_unit(long long u, long long n_units, int grid) {
@@ -230,13 +239,12 @@ __device__ __forceinline__ void normal_cdf_pdf_f64(double z, double& cdf, double
     cdf = 1.0 - pdf * num * rcp_f64(den);
 }
 
-// One ordered pair in FP64 (rsqrt_f64, rcp_f64, the Mills-ratio fit and CUDA's exp). log Phi is not taken
-// per pair: Phi multiplies into lprod (Phi >= 1/2 for d >= 0) and the caller
-// folds log(lprod) into the row's sum every kLogFoldF64Stages stages.
+// One ordered pair in FP64 (rsqrt_f64; log Phi and phi / Phi from the Taylor
+// table of normal_f64, in shared memory): log Phi adds into the row's sum lsum.
 template <int P, bool TRUNC, bool MASKED>
 __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&xj)[P][4], int c, double delta,
-                                         bool valid, double tau, double sqrt_tau, double (&g)[P], double& r2,
-                                         double& lprod) {
+                                         bool valid, double sqrt_tau, double inv_sqrt_tau, const double* tab,
+                                         double (&g)[P], double& r2, double& lsum) {
     double dx[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) dx[q] = xi[q] - xj[q][c];
@@ -252,13 +260,10 @@ __device__ __forceinline__ void pair_f64(const double (&xi)[P], const double (&x
     r2 = fma(res, res, r2);
     double cc;
     if (TRUNC) {
-        const double z = d * sqrt_tau;
-        double cdf, pdf;
-        normal_cdf_pdf_f64(z, cdf, pdf);
-        lprod *= cdf;
-        // (res - pdf / (cdf sqrt_tau)) / d
-        const double den = cdf * sqrt_tau;
-        cc = fma(res, den, -pdf) * rs * rcp_f64(den);
+        double lc, ratio;
+        normal_f64(d * sqrt_tau, tab, lc, ratio);
+        lsum += lc;
+        cc = fma(-ratio, inv_sqrt_tau, res) * rs;  // (res - phi / (Phi sqrt_tau)) / d
     } else {
         cc = res * rs;
     }
@@ -309,9 +314,8 @@ __device__ __forceinline__ void stage_f32(const float* __restrict__ dtile, const
 template <int P, bool TRUNC, bool MASKED, int RW, typename S>
 __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const double* __restrict__ xtile,
                                           const double (&xi)[RW][P], int i0, int j0, int n, int i_lim, int lane,
-                                          double tau,
-                                          double sqrt_tau, double (&g)[RW][P], double (&r2)[RW],
-                                          double (&lprod)[RW]) {
+                                          double sqrt_tau, double inv_sqrt_tau, const double* tab,
+                                          double (&g)[RW][P], double (&r2)[RW], double (&lsum)[RW]) {
     double xj[P][4];
 #pragma unroll
     for (int q = 0; q < P; ++q) {
@@ -337,7 +341,8 @@ __device__ __forceinline__ void stage_f64(const S* __restrict__ dtile, const dou
                 const int i = i0 + r, j = j0 + 4 * lane + c;
                 valid = (j < n) && (i < i_lim) && (i != j) && (dl[c] == dl[c]);
             }
-            pair_f64<P, TRUNC, MASKED>(xi[r], xj, c, dl[c], valid, tau, sqrt_tau, g[r], r2[r], lprod[r]);
+            pair_f64<P, TRUNC, MASKED>(xi[r], xj, c, dl[c], valid, sqrt_tau, inv_sqrt_tau, tab, g[r], r2[r],
+                                       lsum[r]);
         }
     }
 }
@@ -412,6 +417,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
         }
         fence_mbar_init();
     }
+    // FP64 math with truncation: the normal-tail table into shared memory
+    double* tab = sweep_normal_table<!F32 && TRUNC>();
+    if constexpr (!F32 && TRUNC) {
+        const double2* src = reinterpret_cast<const double2*>(a.normal_table_f64);
+        for (int k = threadIdx.x; k < kNormalF64Doubles / 2; k += blockDim.x)
+            reinterpret_cast<double2*>(tab)[k] = __ldg(&src[k]);
+    }
     __syncthreads();
 
     if (warp == kConsumerWarps) {
@@ -455,6 +467,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
     Acc* gpart = static_cast<Acc*>(a.gpart);
     int stage = 0;
     uint32_t phase = 0;
+    const double inv_sqrt_tau = 1.0 / a.sqrt_tau;
     const PairConstsF32 kc{pk(-1.f, -1.f),         pk(a.k_e, a.k_e), pk(a.log2_k2, a.log2_k2),
                            pk(-a.tp0, -a.tp0),     pk(-a.tp1, -a.tp1), pk(-a.tp2, -a.tp2),
                            pk(a.ts0, a.ts0),       pk(a.ts1, a.ts1),   pk(a.ts2, a.ts2)};
@@ -491,7 +504,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
         // FP64 accumulators: gradient, r^2 and logPhi sums per row, and the
         // running product of Phi between log folds.
         C g[RW][P];
-        C r2[RW], acc2[RW], prod64[RW];
+        C r2[RW], acc2[RW];
         // FP32 accumulators (packs): negated gradient, r^2 per fold interval,
         // running product of 1/Phi; and the compensated segment sums.
         f2 g2[RW][P], r2p = pk(0.f, 0.f), prodp = pk(1.f, 1.f);
@@ -499,7 +512,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
         for (int r = 0; r < RW; ++r) {
             r2[r] = C(0);
             acc2[r] = C(0);
-            prod64[r] = C(1);
 #pragma unroll
             for (int q = 0; q < P; ++q) {
                 g[r][q] = C(0);
@@ -525,11 +537,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                     stage_f32<P, TRUNC, false, RW>(dtile, xtile, xi2, grow0, j0, a.n, i_lim, lane, kc, g2, r2p, prodp);
             } else {
                 if (masked)
-                    stage_f64<P, TRUNC, true, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.tau, a.sqrt_tau, g, r2,
-                                                  prod64);
+                    stage_f64<P, TRUNC, true, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.sqrt_tau,
+                                                  inv_sqrt_tau, tab, g, r2, acc2);
                 else
-                    stage_f64<P, TRUNC, false, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.tau, a.sqrt_tau, g,
-                                                   r2, prod64);
+                    stage_f64<P, TRUNC, false, RW>(dtile, xtile, xi, grow0, j0, a.n, i_lim, lane, a.sqrt_tau,
+                                                   inv_sqrt_tau, tab, g, r2, acc2);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[stage]);
@@ -553,15 +565,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
                     two_sum(r2_hi, step_sum, hi, e);
                     r2_hi = hi;
                     r2_lo += e;
-                }
-            } else if (TRUNC) {
-                // 4 factors per row and stage, each in [1/2, 1]: fold well before underflow
-                if ((s + 1) % kLogFoldF64Stages == 0 || s + 1 == steps) {
-#pragma unroll
-                    for (int r = 0; r < RW; ++r) {
-                        acc2[r] += log(prod64[r]);
-                        prod64[r] = C(1);
-                    }
                 }
             }
         }
