@@ -121,6 +121,21 @@ int tmap_f32(CUtensorMap* map, const void* base, long long cols, long long rows,
     return MDSX_OK;
 }
 
+// The plan of the last call on this thread: a sampler calls the sweep again and
+// again with the same problem, and the occupancy query, the CTA-slot count (a
+// pass over every row block) and the two tensor-map encodings then need not be
+// redone. Everything is keyed by what it depends on; the scratch address is
+// still resolved on every call.
+struct NoallocPlan {
+    int device = -1, p = -1, trunc = -1, ctas = 0, sms = 0;  // occupancy of the sweep kernel
+    int n = -1, grid = 0, max_slots = 0;                      // CTA slots per row block
+    const void* delta = nullptr;                              // tensor maps
+    long long delta_ld = -1;
+    const void* x = nullptr;
+    CUtensorMap tmap_delta{}, tmap_x{};
+};
+thread_local NoallocPlan t_plan;
+
 }  // namespace
 
 extern "C" {
@@ -150,20 +165,36 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
     // Same tile plan as the engine's FP32 mode.
     mdsx::KernelShape shape{};
     if (!mdsx::sweep_shape(mdsx::Mode::kF32, p, &shape)) return noalloc_fail(MDSX_EUNSUPPORTED, "dimension not built");
-    int ctas = 0, sms = 0;
-    NOALLOC_CUDA(mdsx::sweep_occupancy(mdsx::Mode::kF32, p, truncation != 0, &ctas));
-    NOALLOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    NoallocPlan& plan = t_plan;
+    const int trunc_key = truncation != 0;
+    if (plan.device != device || plan.p != p || plan.trunc != trunc_key) {
+        plan = NoallocPlan{};
+        NOALLOC_CUDA(mdsx::sweep_occupancy(mdsx::Mode::kF32, p, truncation != 0, &plan.ctas));
+        NOALLOC_CUDA(cudaDeviceGetAttribute(&plan.sms, cudaDevAttrMultiProcessorCount, device));
+        plan.device = device;
+        plan.p = p;
+        plan.trunc = trunc_key;
+    }
     const int rb = shape.rb;
     const int n_row_blocks = (n + rb - 1) / rb;
     const int rows_padded = n_row_blocks * rb;
     const int steps_per_row = (n + mdsx::kStepCols - 1) / mdsx::kStepCols;
     const long long n_units = (long long)n_row_blocks * steps_per_row;
-    const int grid = (int)std::min<long long>(n_units, (long long)sms * std::max(ctas, 1));
-    int max_slots = 1;
-    for (int b = 0; b < n_row_blocks; ++b) {
-        const long long u0 = (long long)b * steps_per_row, u1 = u0 + steps_per_row - 1;
-        max_slots = std::max(max_slots, mdsx::cta_of_unit(u1, n_units, grid) - mdsx::cta_of_unit(u0, n_units, grid) + 1);
+    const int grid = (int)std::min<long long>(n_units, (long long)plan.sms * std::max(plan.ctas, 1));
+    if (plan.n != n || plan.grid != grid) {
+        int max_slots = 1;
+        for (int b = 0; b < n_row_blocks; ++b) {
+            const long long u0 = (long long)b * steps_per_row, u1 = u0 + steps_per_row - 1;
+            max_slots =
+                std::max(max_slots, mdsx::cta_of_unit(u1, n_units, grid) - mdsx::cta_of_unit(u0, n_units, grid) + 1);
+        }
+        plan.n = n;
+        plan.grid = grid;
+        plan.max_slots = max_slots;
+        plan.delta = nullptr;  // the tensor maps depend on n
+        plan.x = nullptr;
     }
+    const int max_slots = plan.max_slots;
     const int x_ld = (int)std::max<long long>((n + mdsx::kStepCols - 1) / mdsx::kStepCols * mdsx::kStepCols, rows_padded);
 
     // Carve the scratch: [out: 4 doubles][counters][row marks][x SoA][gpart][lpart][lrow]
@@ -194,11 +225,20 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
         NOALLOC_CUDA(cudaGetLastError());
     }
 
-    CUtensorMap tmap_delta{}, tmap_x{};
-    rc = tmap_f32(&tmap_delta, d_delta, n, n, delta_ld, mdsx::kStepCols, rb);
-    if (rc) return rc;
-    rc = tmap_f32(&tmap_x, x, n, p, x_ld, mdsx::kStepCols, p);
-    if (rc) return rc;
+    if (plan.delta != d_delta || plan.delta_ld != delta_ld) {
+        plan.delta = nullptr;
+        rc = tmap_f32(&plan.tmap_delta, d_delta, n, n, delta_ld, mdsx::kStepCols, rb);
+        if (rc) return rc;
+        plan.delta = d_delta;
+        plan.delta_ld = delta_ld;
+    }
+    if (plan.x != x) {
+        rc = tmap_f32(&plan.tmap_x, x, n, p, x_ld, mdsx::kStepCols, p);
+        if (rc) return rc;
+        plan.x = x;
+    }
+    const CUtensorMap& tmap_delta = plan.tmap_delta;
+    const CUtensorMap& tmap_x = plan.tmap_x;
 
     mdsx::SweepArgs a{};
     a.n = n;
@@ -233,6 +273,7 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
     a.sums_out = out;
     a.truncation = truncation ? 1 : 0;
     a.err = reinterpret_cast<int*>(out + 3);
+    a.sum_copy = d_sum_of_increments;  // the last CTA writes the caller's sum itself
     // Counters, sums and the error word start at zero on each pass (the
     // preparation kernel clears them for the first).
     double host_out[4];
@@ -242,8 +283,7 @@ int mdsx_sweep_f32_noalloc(const float* d_delta, long long delta_ld, const doubl
             NOALLOC_CUDA(cudaMemsetAsync(counts, 0, ((size_t)n_row_blocks + 1) * sizeof(unsigned), stream));
         }
         NOALLOC_CUDA(mdsx::sweep_launch(mdsx::Mode::kF32, p, truncation != 0, grid, tmap_delta, tmap_x, a, stream));
-        // the sum to the caller and the status to the host, then one synchronisation
-        NOALLOC_CUDA(cudaMemcpyAsync(d_sum_of_increments, out + 2, sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        // the status and the sum to the host, then one synchronisation
         NOALLOC_CUDA(cudaMemcpyAsync(host_out, out, sizeof(host_out), cudaMemcpyDeviceToHost, stream));
         NOALLOC_CUDA(cudaStreamSynchronize(stream));
         int dev_err = 0;

@@ -89,6 +89,7 @@ struct SweepArgs {
     int truncation;
     int* err;
     const double* normal_table_f64;  // FP64 math with truncation: normal_f64_table (kNormalF64Doubles)
+    double* sum_copy;                // optional: also receives getSumOfIncrements() (the caller's buffer)
 };
 
 // The FP64 normal-tail table in shared memory (a static array of the kernel
@@ -680,6 +681,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(C) == 4 ? MDSX_F32_MIN_CTAS :
             // src/NewMultiDimensionalScaling.hpp:198-202 and :554-557: halve the
             // ordered-pair total; without truncation scale by 0.5 * tau.
             a.sums_out[2] = a.truncation ? 0.5 * (0.5 * a.tau * tr2 + tlog) : 0.5 * a.tau * (0.5 * tr2);
+            if (a.sum_copy) *a.sum_copy = a.sums_out[2];
             *a.done_count = 0u;
         }
     }
