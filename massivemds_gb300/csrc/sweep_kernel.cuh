@@ -34,8 +34,9 @@
 // giving 1/Phi); logPhi summed as log2 of running products of 1/Phi (one lg2
 // per 64 pairs); r^2 sums compensated with TwoSum; per-tile partials promoted to
 // FP64 for every reduction above the warp. FP64 mode: pair arithmetic in FP64
-// with CUDA's double exp/log, Phi from our Mills-ratio fit (normal_cdf_pdf_f64)
-// and Newton-refined reciprocals (rcp_f64, rsqrt_f64).
+// with a Newton-refined rsqrt_f64, and log Phi and phi / Phi from the Taylor
+// table of normal_dd.h (normal_f64, in shared memory); normal_cdf_pdf_f64 (our
+// Mills-ratio fit with CUDA's exp) remains for the FP64 self-test.
 #pragma once
 
 #include <cstdint>
@@ -229,7 +230,8 @@ __device__ __forceinline__ void pair2_f32(const f2 (&xi)[P], const f2 (&xj)[P], 
     for (int q = 0; q < P; ++q) g[q] = ffma2(c, dx[q], g[q]);
 }
 
-// Normal CDF and density at z >= 0 in FP64 with one exponential:
+// Normal CDF and density at z >= 0 in FP64 with one exponential (the FP64
+// helpers' self-test, mdsx_selftest_math_f64; the sweeps use normal_f64):
 // Phi(z) = 1 - Q(z), Q(z) = phi(z) R(z) with R the Mills ratio from our rational
 // fit (normal_mills_f64.h, evaluated at min(z, 8.5), where Q < 1e-17 beyond);
 // the exponential of the density serves both. |Phi - Phi_exact| <= 1e-15.
