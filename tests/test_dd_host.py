@@ -1,8 +1,9 @@
 """Host checks of the double-float arithmetic and the double-float normal tail
 table (massivemds_gb300/csrc/dd.h, normal_dd.h), compiled with the host C++
 compiler: each operation against long double, and log Phi(z), phi(z) / Phi(z)
-on [0, 9] against the C library's erfc, exp and log1p in long double
-(tests/dd_check.cpp prints the measured errors and their bounds). No GPU."""
+on [0, 9] against the C library's erfc, exp and log1p in long double, from the
+double-float table and from the FP64 sweeps' double table (tests/dd_check.cpp
+prints the measured errors and their bounds). No GPU."""
 import os
 import shutil
 import subprocess
@@ -22,10 +23,13 @@ def test_double_float_ops_and_normal_table(tmp_path):
                    check=True)
     r = subprocess.run([exe], capture_output=True, text=True)
     lines = dict((ln.split()[0], (float(ln.split()[1]), float(ln.split()[2]))) for ln in r.stdout.splitlines())
-    for name in ("add", "mul", "sqr", "fma", "rsqrt", "rcp", "div", "normal_logcdf_abs", "normal_ratio_abs"):
+    for name in ("add", "mul", "sqr", "fma", "rsqrt", "rcp", "div", "acc_fma_20000", "acc_sqr_20000",
+                 "normal_logcdf_abs", "normal_ratio_abs", "normal_f64_logcdf_abs", "normal_f64_ratio_abs"):
         assert name in lines, r.stdout
     assert r.returncode == 0, r.stdout
     assert lines["normal_logcdf_abs"][0] < 5e-14 and lines["normal_ratio_abs"][0] < 5e-14
+    # the FP64 sweeps' table (normal_f64): FP64-grade
+    assert lines["normal_f64_logcdf_abs"][0] < 5e-16 and lines["normal_f64_ratio_abs"][0] < 5e-16
 
 
 def test_double_float_flag_excludes_float(mdsx_lib):
