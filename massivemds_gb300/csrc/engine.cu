@@ -174,6 +174,26 @@ int plan_pairs(mdsx_engine* e) {
     return MDSX_OK;
 }
 
+// The normal-tail tables on the host, computed once per process (the series
+// coefficients take long-double erfc, exp and log1p, which are slow where long
+// double is a software type) and copied to each engine that needs them.
+const std::vector<double>& normal_f64_table_host() {
+    static const std::vector<double> table = [] {
+        std::vector<double> t(mdsx::kNormalF64Doubles);
+        mdsx::normal_f64_table(t.data());
+        return t;
+    }();
+    return table;
+}
+const std::vector<float>& normal_dd_table_host() {
+    static const std::vector<float> table = [] {
+        std::vector<float> t(mdsx::kNormalDDFloats);
+        mdsx::normal_dd_table(t.data());
+        return t;
+    }();
+    return table;
+}
+
 int plan_and_allocate(mdsx_engine* e) {
     if (!mdsx::sweep_shape(e->mode, e->p, &e->shape))
         return fail(e, MDSX_EUNSUPPORTED, "embedding dimension not built (1..MDSX_MAX_DIMENSION)");
@@ -246,8 +266,7 @@ int plan_and_allocate(mdsx_engine* e) {
     }
     // the FP64 math's normal-tail table (pair and row-block schedules)
     if (!e->dd && e->mode != Mode::kF32 && e->trunc) {
-        std::vector<double> table(mdsx::kNormalF64Doubles);
-        mdsx::normal_f64_table(table.data());
+        const std::vector<double>& table = normal_f64_table_host();
         MDSX_CUDA(e, mdsx::device_malloc(&e->d_normal_table_f64, table.size() * sizeof(double)));
         MDSX_CUDA(e, cudaMemcpy(e->d_normal_table_f64, table.data(), table.size() * sizeof(double),
                                 cudaMemcpyHostToDevice));
@@ -257,8 +276,7 @@ int plan_and_allocate(mdsx_engine* e) {
             return fail(e, MDSX_EUNSUPPORTED,
                         "double-float pair math runs on the unordered-pair schedule only (P <= 6, whole matrix)");
         if (e->trunc) {
-            std::vector<float> table(mdsx::kNormalDDFloats);
-            mdsx::normal_dd_table(table.data());
+            const std::vector<float>& table = normal_dd_table_host();
             MDSX_CUDA(e, mdsx::device_malloc(&e->d_normal_table, table.size() * sizeof(float)));
             MDSX_CUDA(e, cudaMemcpy(e->d_normal_table, table.data(), table.size() * sizeof(float),
                                     cudaMemcpyHostToDevice));
