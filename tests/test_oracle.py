@@ -164,3 +164,47 @@ def test_planted_error_is_detected():
     wrong[3, 7] += 0.5  # a perturbed observation in row 3
     g2 = oracle.gradient(wrong, x, 1.0)
     assert _grad_rel(g2, g) > 1e-6
+
+
+def _symmetric_delta(rng, n, nan_pairs=0):
+    y = rng.standard_normal((n, 10))
+    d = np.sqrt(((y[:, None] - y[None]) ** 2).sum(-1))
+    e = np.triu(rng.standard_normal((n, n)) * 0.05, 1)
+    d = np.clip(d + e + e.T, 0.0, None)
+    for _ in range(nan_pairs):
+        i, j = rng.choice(n, 2, replace=False)
+        d[i, j] = d[j, i] = np.nan
+    return d
+
+
+@pytest.mark.parametrize("trunc", [True, False])
+def test_oracle_distance_invariances(trunc):
+    """The likelihood depends on the locations only through their pairwise
+    distances: a translation or a rotation of every location leaves the sum and
+    the gradient (rotated with them) unchanged, relabelling the locations
+    permutes the gradient, and with a symmetric delta the gradient summed over
+    all locations vanishes (each pair term enters its two rows with opposite
+    signs, src/NewMultiDimensionalScaling.hpp:421-456)."""
+    rng = np.random.default_rng(11)
+    n, p, tau = 180, 3, 0.7
+    delta = _symmetric_delta(rng, n, nan_pairs=5)
+    x = 2.0 * rng.standard_normal((n, p))
+    s, g = oracle.evaluate(delta, x, tau, trunc)
+    g = np.asarray(g).reshape(n, p)
+
+    net = np.abs(g.sum(axis=0)) / np.abs(g).sum(axis=0)
+    assert net.max() < 1e-13, net
+
+    s_t, g_t = oracle.evaluate(delta, x + np.array([0.75, -1.5, 2.25]), tau, trunc)
+    assert _rel(s_t, s) < 1e-12
+    assert _grad_rel(np.asarray(g_t).reshape(n, p), g) < 1e-10
+
+    q, _ = np.linalg.qr(rng.standard_normal((p, p)))
+    s_r, g_r = oracle.evaluate(delta, x @ q, tau, trunc)
+    assert _rel(s_r, s) < 1e-12
+    assert _grad_rel(np.asarray(g_r).reshape(n, p), g @ q) < 1e-10
+
+    perm = rng.permutation(n)
+    s_p, g_p = oracle.evaluate(delta[np.ix_(perm, perm)], x[perm], tau, trunc)
+    assert _rel(s_p, s) < 1e-12
+    assert _grad_rel(np.asarray(g_p).reshape(n, p), g[perm]) < 1e-12
