@@ -7,7 +7,11 @@
 //   - every column-block slot and likelihood slot a CTA writes lies in its table,
 //     and every slot the finish kernel reads was written;
 //   - every unordered pair i > j of every instance is covered exactly once
-//     (instances up to 700 locations).
+//     (instances up to 700 locations);
+//   - the finish kernel's blocks (pair_finish_block, every FinishShape: P = 1..6,
+//     FP32 and FP64 partials) read only inside the row- and column-partial
+//     buffers as the engine sizes them, read every row partial and every column
+//     partial of a real column once, and write every gradient entry once.
 // Prints "ok" and exits 0, or prints the first failure and exits 1.
 #include <cstdio>
 #include <cstdlib>
@@ -119,8 +123,95 @@ static void check(const std::vector<int>& ns, long long max_grid) {
     }
 }
 
+// The finish of one sweep over an N-location instance, replaying the index
+// arithmetic of pair_finish_block (pair_kernel.cuh) for every block and thread.
+template <int P, typename Part>
+static void check_finish(int n, long long max_grid) {
+    using FS = mdsx::FinishShape<P, Part>;
+    static_assert(FS::kGroups * FS::kOut <= FS::kThreads, "finish block holds its groups");
+    static_assert(FS::kRows * FS::kSplit == kPairRows, "row split covers a chunk");
+    const mdsx::PairPlan plan = mdsx::pair_plan({n}, max_grid);
+    const mdsx::PairInstancePlan& q = plan.inst[0];
+    const int nc = q.nc, nb = q.nb;
+    const size_t row_size = (size_t)q.units * kPairRows * P;  // engine.cu's allocations
+    const size_t col_size = (size_t)nb * q.max_slots * mdsx::kPairWarps * P * kPairCols;
+    std::vector<unsigned char> row_read(row_size, 0), col_read(col_size, 0), grad_written((size_t)n * P, 0);
+    const int blocks = mdsx::pair_finish_blocks<P, Part>(nc);
+    CHECK(blocks == 1 + nc * FS::kSplit, "finish grid");
+    for (int blk = 1; blk < blocks; ++blk) {
+        const int ci = (blk - 1) / FS::kSplit;
+        const int I = nc - 1 - ci;
+        const int h0 = (blk - 1 - ci * FS::kSplit) * FS::kRows;
+        CHECK(I >= 0 && I < nc && h0 >= 0 && h0 + FS::kRows <= kPairRows, "block %d", blk);
+        for (int t = 0; t < FS::kThreads; ++t) {
+            const int g = t / FS::kOut, o = t - g * FS::kOut;
+            if (g < FS::kGroups) {
+                const int j_max = I >> 2;
+                for (int J0 = g; J0 <= j_max; J0 += FS::kGroups * FS::kChunk)
+                    for (int k = 0; k < FS::kChunk; ++k) {
+                        const int J = J0 + FS::kGroups * k;
+                        if (J > j_max) continue;
+                        const long long u = pair_units_before(J, nc) + (I - 4 * J);
+                        const size_t idx = (size_t)u * (kPairRows * P) + h0 * P + o;
+                        CHECK(u >= 0 && u < q.units && idx < row_size, "row partial (%d, %d) P %d", J, I, P);
+                        ++row_read[idx];
+                    }
+                const int J = I >> 2, r = o / P, qd = o - r * P, jj = (I & 3) * kPairRows + h0 + r;
+                CHECK(J < nb && jj < kPairCols, "column block %d", J);
+                const int n_e = q.j_slots[J] * mdsx::kPairWarps;
+                CHECK(q.j_slots[J] <= q.max_slots, "slots of %d", J);
+                for (int e0 = g; e0 < n_e; e0 += FS::kGroups * FS::kColChunk)
+                    for (int k = 0; k < FS::kColChunk; ++k) {
+                        const int e = e0 + FS::kGroups * k;
+                        if (e >= n_e) continue;
+                        const size_t idx = ((size_t)J * q.max_slots * mdsx::kPairWarps + e) * (P * kPairCols) +
+                                           qd * kPairCols + jj;
+                        CHECK(idx < col_size, "column partial J %d e %d", J, e);
+                        ++col_read[idx];
+                    }
+            }
+            if (t < FS::kOut) {
+                const int row = I * kPairRows + h0 + t / P;
+                if (row < n) {
+                    const size_t idx = (size_t)(I * kPairRows + h0) * P + t;
+                    CHECK(idx < (size_t)n * P, "gradient index");
+                    ++grad_written[idx];
+                }
+            }
+        }
+    }
+    for (size_t i = 0; i < row_size; ++i) CHECK(row_read[i] == 1, "row partial %zu read %d times", i, row_read[i]);
+    for (int J = 0; J < nb; ++J)
+        for (int e = 0; e < q.max_slots * mdsx::kPairWarps; ++e)
+            for (int qd = 0; qd < P; ++qd)
+                for (int jj = 0; jj < kPairCols; ++jj) {
+                    const size_t idx = ((size_t)J * q.max_slots * mdsx::kPairWarps + e) * (P * kPairCols) +
+                                       qd * kPairCols + jj;
+                    const bool real = e < q.j_slots[J] * mdsx::kPairWarps && J * kPairCols + jj < nc * kPairRows;
+                    CHECK(col_read[idx] == (real ? 1 : 0), "column partial (J %d, e %d, q %d, col %d) read %d times", J,
+                          e, qd, jj, col_read[idx]);
+                }
+    for (size_t i = 0; i < grad_written.size(); ++i)
+        CHECK(grad_written[i] == 1, "gradient entry %zu written %d times", i, grad_written[i]);
+}
+
+template <typename Part>
+static void check_finish_all(int n, long long max_grid) {
+    check_finish<1, Part>(n, max_grid);
+    check_finish<2, Part>(n, max_grid);
+    check_finish<3, Part>(n, max_grid);
+    check_finish<4, Part>(n, max_grid);
+    check_finish<5, Part>(n, max_grid);
+    check_finish<6, Part>(n, max_grid);
+}
+
 int main() {
     std::mt19937 rng(7);
+    for (int n : {1, 2, 31, 32, 33, 127, 128, 129, 300, 641, 1000, 4099})
+        for (long long g : {1LL, 17LL, 152LL, 304LL}) {
+            check_finish_all<float>(n, g);
+            check_finish_all<double>(n, g);
+        }
     const long long grids[] = {1, 2, 5, 17, 152, 304};
     for (int n : {1, 2, 31, 32, 33, 127, 128, 129, 300, 641, 700})
         for (long long g : grids) check({n}, g);

@@ -1,7 +1,9 @@
 """CPU test of the unordered-pair plan (massivemds_gb300/csrc/pair_plan.h): builds
 tests/pair_plan_check.cu (host code only) with nvcc and runs it. The driver walks
 every CTA's unit range the way the pair kernels do and checks coverage of every
-pair, the producer/consumer unit order and the slot tables."""
+pair, the producer/consumer unit order and the slot tables; it replays the finish
+kernel's index arithmetic for every finish shape and checks its reads stay inside
+the partial buffers, read each partial once and write each gradient entry once."""
 import os
 import shutil
 import subprocess
